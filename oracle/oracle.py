@@ -1,0 +1,255 @@
+"""Python front end of the CPU oracle (test infrastructure only).
+
+The oracle is a plain-C restatement of the ArborX BoundingVolumeHierarchy hot
+path (``oracle/abx_oracle.c``; each C function cites the reference file:line it
+follows).  It is the CHECKER for the CUDA library: only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg import this
+module.  Nothing in ``arborx_gb300`` imports it.
+
+Parity status: pinned by the known-answer vectors of the reference's own tests
+(``tests/golden/``) plus exact brute-force cross-checks; the reference itself
+cannot be compiled here (Kokkos >= 4.5 is absent).
+"""
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "libabx_oracle.so")
+
+INTERNAL_DTYPE = np.dtype([("left_child", "<i4"), ("rope", "<i4"), ("box", "<f4", (6,))])
+LEAF_DTYPE = np.dtype([("rope", "<i4"), ("value", "<i4")])
+assert INTERNAL_DTYPE.itemsize == 32 and LEAF_DTYPE.itemsize == 8
+
+KIND_POINT, KIND_SPHERE, KIND_BOX = 0, 1, 2
+MODE_ARBORX, MODE_ORDERED = 0, 1
+
+_lib = None
+
+
+def build_oracle(verbose=False):
+    """Compile the C oracle with its Makefile (gcc, no GPU needed)."""
+    cmd = ["make", "-s", "-C", _HERE]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+    if verbose and out.stdout:
+        print(out.stdout)
+    return _LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(
+            os.path.join(_HERE, "abx_oracle.c")
+        ):
+            build_oracle()
+        L = ctypes.CDLL(_LIB_PATH)
+        P = ctypes.c_void_p
+        I64 = ctypes.c_int64
+        I32 = ctypes.c_int32
+        I = ctypes.c_int
+        L.abxo_expand_bits64.restype = ctypes.c_uint64
+        L.abxo_expand_bits64.argtypes = [ctypes.c_uint64, I]
+        L.abxo_expand_bits32.restype = ctypes.c_uint32
+        L.abxo_expand_bits32.argtypes = [ctypes.c_uint32, I]
+        L.abxo_morton64.restype = ctypes.c_uint64
+        L.abxo_morton64.argtypes = [P, I]
+        L.abxo_morton32.restype = ctypes.c_uint32
+        L.abxo_morton32.argtypes = [P, I]
+        L.abxo_scene_bounds.argtypes = [P, I64, I, P]
+        L.abxo_morton64_codes.argtypes = [P, I64, I, P, P]
+        L.abxo_morton32_codes.argtypes = [P, I64, I, P, P]
+        L.abxo_sort_u64.argtypes = [P, I64, P]
+        L.abxo_sort_u32.argtypes = [P, I64, P]
+        L.abxo_generate_hierarchy.argtypes = [P, I64, I, P, P, P, P]
+        L.abxo_build.argtypes = [P, I64, I, P, P, P, P, P]
+        L.abxo_spatial_count.restype = I64
+        L.abxo_spatial_count.argtypes = [I64, I, P, P, P, I, P, I64, P]
+        L.abxo_spatial_fill.argtypes = [I64, I, P, P, P, I, P, I64, P, P]
+        L.abxo_nearest.restype = I64
+        L.abxo_nearest.argtypes = [I64, I, P, P, P, P, I64, P, I32, I, P, P, P]
+        L.abxo_knn_brute.argtypes = [P, I64, I, P, I64, I32, P, P]
+        L.abxo_spatial_brute.restype = I64
+        L.abxo_spatial_brute.argtypes = [P, I64, I, I, P, I64, P, P]
+        L.abxo_exclusive_scan_i32.argtypes = [P, I64, P]
+        L.abxo_num_threads.restype = I
+        L.abxo_set_num_threads.argtypes = [I]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _f32(a, cols):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    if a.size == 0:
+        return a.reshape(0, cols)
+    return a.reshape(-1, cols)
+
+
+def num_threads():
+    return lib().abxo_num_threads()
+
+
+def set_num_threads(n):
+    lib().abxo_set_num_threads(int(n))
+
+
+def expand_bits64(x, n_zero):
+    return int(lib().abxo_expand_bits64(int(x), int(n_zero)))
+
+
+def expand_bits32(x, n_zero):
+    return int(lib().abxo_expand_bits32(int(x), int(n_zero)))
+
+
+def morton64(p):
+    a = np.ascontiguousarray(p, dtype=np.float32).reshape(-1)
+    return int(lib().abxo_morton64(_p(a), a.size))
+
+
+def morton32(p):
+    a = np.ascontiguousarray(p, dtype=np.float32).reshape(-1)
+    return int(lib().abxo_morton32(_p(a), a.size))
+
+
+def scene_bounds(geom, is_box=False):
+    g = _f32(geom, 6 if is_box else 3)
+    out = np.empty(6, np.float32)
+    lib().abxo_scene_bounds(_p(g), g.shape[0], int(is_box), _p(out))
+    return out
+
+
+def morton64_codes(geom, scene, is_box=False):
+    g = _f32(geom, 6 if is_box else 3)
+    s = np.ascontiguousarray(scene, dtype=np.float32)
+    out = np.empty(g.shape[0], np.uint64)
+    lib().abxo_morton64_codes(_p(g), g.shape[0], int(is_box), _p(s), _p(out))
+    return out
+
+
+def morton32_codes(geom, scene, kind):
+    g = _f32(geom, {KIND_POINT: 3, KIND_SPHERE: 4, KIND_BOX: 6}[kind])
+    s = np.ascontiguousarray(scene, dtype=np.float32)
+    out = np.empty(g.shape[0], np.uint32)
+    lib().abxo_morton32_codes(_p(g), g.shape[0], int(kind), _p(s), _p(out))
+    return out
+
+
+def sort_u64(keys):
+    k = np.array(keys, dtype=np.uint64, copy=True)
+    perm = np.empty(k.size, np.uint32)
+    lib().abxo_sort_u64(_p(k), k.size, _p(perm))
+    return k, perm
+
+
+def sort_u32(keys):
+    k = np.array(keys, dtype=np.uint32, copy=True)
+    perm = np.empty(k.size, np.uint32)
+    lib().abxo_sort_u32(_p(k), k.size, _p(perm))
+    return k, perm
+
+
+def generate_hierarchy(geom, perm, sorted_codes, is_box=False):
+    g = _f32(geom, 6 if is_box else 3)
+    n = g.shape[0]
+    perm = np.ascontiguousarray(perm, dtype=np.uint32)
+    codes = np.ascontiguousarray(sorted_codes, dtype=np.uint64)
+    leaves = np.zeros(n, LEAF_DTYPE)
+    internal = np.zeros(max(n - 1, 0), INTERNAL_DTYPE)
+    lib().abxo_generate_hierarchy(_p(g), n, int(is_box), _p(perm), _p(codes), _p(leaves), _p(internal))
+    return leaves, internal
+
+
+def exclusive_scan(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    out = np.empty_like(a)
+    lib().abxo_exclusive_scan_i32(_p(a), a.size, _p(out))
+    return out
+
+
+class OracleTree:
+    """ArborX BVH built on the CPU: tree arrays in the reference layout."""
+
+    def __init__(self, geom, is_box=False):
+        self.is_box = bool(is_box)
+        self.geom = _f32(geom, 6 if is_box else 3)
+        n = self.geom.shape[0]
+        self.n = n
+        self.bounds = np.empty(6, np.float32)
+        self.sorted_codes = np.zeros(n, np.uint64)
+        self.perm = np.zeros(n, np.uint32)
+        self.leaves = np.zeros(n, LEAF_DTYPE)
+        self.internal = np.zeros(max(n - 1, 0), INTERNAL_DTYPE)
+        lib().abxo_build(
+            _p(self.geom), n, int(self.is_box), _p(self.bounds), _p(self.sorted_codes),
+            _p(self.perm), _p(self.leaves), _p(self.internal),
+        )
+
+    def _tree_args(self):
+        return (self.n, int(self.is_box), _p(self.geom), _p(self.leaves), _p(self.internal))
+
+    def spatial(self, kind, preds):
+        """CRS (offsets, indices) of intersects(Sphere|Box) predicates."""
+        preds = _f32(preds, 4 if kind == KIND_SPHERE else 6)
+        nq = preds.shape[0]
+        offsets = np.zeros(nq + 1, np.int32)
+        total = lib().abxo_spatial_count(*self._tree_args(), int(kind), _p(preds), nq, _p(offsets))
+        indices = np.empty(total, np.int32)
+        lib().abxo_spatial_fill(*self._tree_args(), int(kind), _p(preds), nq, _p(offsets), _p(indices))
+        return offsets, indices
+
+    def nearest(self, queries, k, mode=MODE_ORDERED):
+        """CRS (offsets, indices, distances) of nearest(Point, k) predicates.
+
+        ``k`` is an int or one int per query.  mode MODE_ARBORX restates the
+        reference's tie behaviour; MODE_ORDERED keeps the k smallest
+        (distance, index) pairs in ascending order (this library's rule).
+        """
+        q = _f32(queries, 3)
+        nq = q.shape[0]
+        kq = None
+        k_scalar = 0
+        if np.ndim(k) == 0:
+            k_scalar = int(k)
+            total = nq * max(0, min(k_scalar, self.n))
+        else:
+            kq = np.ascontiguousarray(k, dtype=np.int32)
+            total = int(np.minimum(np.maximum(kq, 0), self.n).sum())
+        offsets = np.zeros(nq + 1, np.int32)
+        indices = np.empty(total, np.int32)
+        dist = np.empty(total, np.float32)
+        r = lib().abxo_nearest(
+            *self._tree_args(), _p(q), nq, _p(kq), k_scalar, int(mode), _p(offsets), _p(indices), _p(dist)
+        )
+        if r < 0:
+            raise RuntimeError("oracle nearest traversal overflowed its 64-entry stack")
+        return offsets, indices, dist
+
+
+def knn_brute(geom, queries, k, is_box=False):
+    g = _f32(geom, 6 if is_box else 3)
+    q = _f32(queries, 3)
+    kk = max(0, min(int(k), g.shape[0]))
+    idx = np.empty((q.shape[0], kk), np.int32)
+    dist = np.empty((q.shape[0], kk), np.float32)
+    lib().abxo_knn_brute(_p(g), g.shape[0], int(is_box), _p(q), q.shape[0], int(k), _p(idx), _p(dist))
+    return idx, dist
+
+
+def spatial_brute(geom, kind, preds, is_box=False):
+    g = _f32(geom, 6 if is_box else 3)
+    p = _f32(preds, 4 if kind == KIND_SPHERE else 6)
+    nq = p.shape[0]
+    offsets = np.zeros(nq + 1, np.int32)
+    total = lib().abxo_spatial_brute(_p(g), g.shape[0], int(is_box), int(kind), _p(p), nq, _p(offsets), None)
+    indices = np.empty(total, np.int32)
+    lib().abxo_spatial_brute(_p(g), g.shape[0], int(is_box), int(kind), _p(p), nq, _p(offsets), _p(indices))
+    return offsets, indices

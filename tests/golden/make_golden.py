@@ -1,0 +1,160 @@
+"""Generate tests/golden/reference_kats.json from the reference's test files.
+
+Run in a container that has the ArborX sources mounted:
+
+    python tests/golden/make_golden.py /root/reference
+
+The known-answer vectors are read out of the reference's Boost.Test sources as
+text (regular expressions over the assertion lines), so the fixture follows
+the reference exactly; the structured degenerate / policy cases whose inputs
+are spelled as C++ initialiser lists are transcribed below with the file:line
+they come from.  The JSON is committed; tests never read the reference tree.
+"""
+
+import json
+import os
+import re
+import sys
+
+
+def _read(root, rel):
+    with open(os.path.join(root, rel)) as f:
+        return f.read()
+
+
+def morton_kats(root):
+    """test/tstDetailsMortonCodes.cpp:22-82."""
+    src = _read(root, "test/tstDetailsMortonCodes.cpp")
+    x32 = int(re.search(r"unsigned x = 0b([01]+)u;", src).group(1), 2)
+    y64 = int(re.search(r"unsigned long long y = 0b([01]+)llu;", src).group(1), 2)
+    expand32, expand64 = [], []
+    for m in re.finditer(r"expandBitsBy<(\d)>\((x|y)\) ==\s+0b([01]+)(u|llu)\);", src):
+        n, var, bits = int(m.group(1)), m.group(2), int(m.group(3), 2)
+        (expand32 if var == "x" else expand64).append(
+            {"n_zero": n, "input": x32 if var == "x" else y64, "expected": bits}
+        )
+    morton = []
+    for m in re.finditer(r"morton(32|64)\(Point\{([^}]*)\}\) == 0x([0-9a-f]+)(u|llu)\);", src):
+        coords = [float(c.strip().rstrip("f")) for c in m.group(2).split(",")]
+        morton.append({"bits": int(m.group(1)), "point": coords, "expected": int(m.group(3), 16)})
+    assert len(expand32) == 10 and len(expand64) == 10 and len(morton) == 22
+    return {"expand_bits32": expand32, "expand_bits64": expand64, "morton": morton}
+
+
+def karras_example(root):
+    """test/tstDetailsTreeConstruction.cpp:217-269 (Karras' 8-key example)."""
+    src = _read(root, "test/tstDetailsTreeConstruction.cpp")
+    block = src[src.index("example_tree_construction"):]
+    codes = re.search(r"std::vector<std::string> s\{([^}]*)\}", block).group(1)
+    codes = [int(c, 2) for c in re.findall(r'"([01]+)"', codes)]
+    ref = re.search(r"ref << ((?:\"[IL]\d\"\s*(?:<<\s*)?)+)", block).group(1)
+    dfs = "".join(re.findall(r'"([IL]\d)"', ref))
+    assert len(codes) == 8 and len(dfs) == 2 * 15
+    return {"sorted_codes": codes, "dfs": dfs}
+
+
+def assign_morton_codes(root):
+    """test/tstDetailsTreeConstruction.cpp:33-102: 7 points, their scene box
+    and Morton64 codes 4*e(i) + 2*e(j) + e(k) of the anchor cells."""
+    src = _read(root, "test/tstDetailsTreeConstruction.cpp")
+    assert "{{1.33, 2.33, 3.33}}" in src and "{{N - 1, N - 1, N - 1}}" in src
+    N = 1 << 21
+    points = [
+        [0.0, 0.0, 0.0],
+        [0.25, 0.75, 0.25],
+        [0.75, 0.25, 0.25],
+        [0.75, 0.75, 0.25],
+        [1.33, 2.33, 3.33],
+        [1.66, 2.66, 3.66],
+        [float(N), float(N), float(N)],
+    ]
+    anchors = [[0, 0, 0]] * 4 + [[1, 2, 3]] * 2 + [[N - 1, N - 1, N - 1]]
+    return {"points": points, "scene": [0.0, 0.0, 0.0, float(N), float(N), float(N)], "anchors": anchors}
+
+
+def degenerate_cases():
+    """test/tstQueryTreeDegenerate.cpp:25-446 and
+    test/tstQueryTreeTraversalPolicy.cpp:32-202, transcribed.  Leaves are
+    boxes [min xyz, max xyz]; E is the default (empty) box; spheres are
+    [cx, cy, cz, r]; nearest queries are [x, y, z, k]."""
+    E = "empty"
+    unit = [0, 0, 0, 1, 1, 1]
+    p0 = [0, 0, 0, 0, 0, 0]
+    p1 = [1, 1, 1, 1, 1, 1]
+    cases = [
+        # empty tree (:25-123)
+        {"cite": "tstQueryTreeDegenerate.cpp:57-83", "leaves": [], "kind": "box",
+         "queries": [E, E], "indices": [], "offsets": [0, 0, 0]},
+        {"cite": "tstQueryTreeDegenerate.cpp:85-101", "leaves": [], "kind": "sphere",
+         "queries": [[0, 0, 0, 1], [1, 1, 1, 2]], "indices": [], "offsets": [0, 0, 0]},
+        {"cite": "tstQueryTreeDegenerate.cpp:115-122", "leaves": [], "kind": "nearest",
+         "queries": [[0, 0, 0, 1], [1, 1, 1, 2]], "indices": [], "offsets": [0, 0, 0]},
+        # single leaf (:125-223)
+        {"cite": "tstQueryTreeDegenerate.cpp:147-153", "leaves": [unit], "kind": "box",
+         "queries": [[5, 5, 5, 5, 5, 5], [.5, .5, .5, .5, .5, .5]], "indices": [0], "offsets": [0, 0, 1]},
+        {"cite": "tstQueryTreeDegenerate.cpp:161-168", "leaves": [unit], "kind": "sphere",
+         "queries": [[0, 0, 0, 1], [1, 1, 1, 3], [5, 5, 5, 2]], "indices": [0, 0], "offsets": [0, 1, 2, 2]},
+        {"cite": "tstQueryTreeDegenerate.cpp:197-200", "leaves": [unit], "kind": "nearest",
+         "queries": [[0, 0, 0, 3], [4, 5, 1, 1]], "indices": [0, 0], "offsets": [0, 1, 2]},
+        {"cite": "tstQueryTreeDegenerate.cpp:202-209", "leaves": [unit], "kind": "nearest",
+         "queries": [[0, 0, 0, 1], [1, 1, 1, 2], [2, 2, 2, 3]], "indices": [0, 0, 0], "offsets": [0, 1, 2, 3]},
+        # two leaves (:212-323)
+        {"cite": "tstQueryTreeDegenerate.cpp:240-245", "leaves": [p0, p1], "kind": "box",
+         "queries": [E], "indices": [], "offsets": [0, 0]},
+        {"cite": "tstQueryTreeDegenerate.cpp:248-252", "leaves": [p0, p1], "kind": "box",
+         "queries": [unit], "indices": [1, 0], "offsets": [0, 2]},
+        {"cite": "tstQueryTreeDegenerate.cpp:255-259", "leaves": [p0, p1], "kind": "box",
+         "queries": [[.5, .5, .5, 1.5, 1.5, 1.5]], "indices": [1], "offsets": [0, 1]},
+        {"cite": "tstQueryTreeDegenerate.cpp:262-267", "leaves": [p0, p1], "kind": "box",
+         "queries": [E, E], "indices": [], "offsets": [0, 0, 0]},
+        {"cite": "tstQueryTreeDegenerate.cpp:270-275", "leaves": [p0, p1], "kind": "box",
+         "queries": [E, p0], "indices": [0], "offsets": [0, 0, 1]},
+        {"cite": "tstQueryTreeDegenerate.cpp:314-320", "leaves": [p0, p1], "kind": "nearest",
+         "queries": [[0, 0, 0, 2], [1, 0, 0, 4]], "indices": [0, 1, 0, 1], "offsets": [0, 2, 4]},
+        # duplicated leaves (:325-361)
+        {"cite": "tstQueryTreeDegenerate.cpp:342-359", "leaves": [p0, p1, p1, p1], "kind": "sphere",
+         "queries": [[0, 0, 0, 1], [1, 1, 1, 1], [.5, .5, .5, 1]],
+         "indices": [0, 1, 2, 3, 0, 1, 2, 3], "offsets": [0, 1, 4, 8]},
+        # buffer optimisation (tstQueryTreeTraversalPolicy.cpp:32-130)
+        {"cite": "tstQueryTreeTraversalPolicy.cpp:43-60", "leaves": [p0, [1, 0, 0, 1, 0, 0], [2, 0, 0, 2, 0, 0], [3, 0, 0, 3, 0, 0]],
+         "kind": "box", "queries": [E, [0, 0, 0, 3, 3, 3], E], "indices": [0, 1, 2, 3], "offsets": [0, 0, 4, 4],
+         "buffer_sizes_ok": [0, -4, 5, -5, 1], "buffer_sizes_throw": [-1]},
+        # unsorted predicates (:132-202)
+        {"cite": "tstQueryTreeTraversalPolicy.cpp:152-174", "leaves": [p0, p1, [2, 2, 2, 2, 2, 2], [3, 3, 3, 3, 3, 3]],
+         "kind": "box", "queries": [[2, 2, 2, 3, 3, 3], [0, 0, 0, 1, 1, 1]], "indices": [2, 3, 0, 1], "offsets": [0, 2, 4]},
+        {"cite": "tstQueryTreeTraversalPolicy.cpp:177-199", "leaves": [p0, p1, [2, 2, 2, 2, 2, 2], [3, 3, 3, 3, 3, 3]],
+         "kind": "nearest", "queries": [[2.5, 2.5, 2.5, 2], [.5, .5, .5, 2]], "indices": [2, 3, 0, 1], "offsets": [0, 2, 4]},
+    ]
+    return cases
+
+
+def crs_query_impl():
+    """test/tstDetailsCrsGraphWrapperImpl.cpp:49-101: predicate i reports
+    values 0..i-1; two-pass CRS with hard preallocation 2(n+1)."""
+    n = 10
+    offsets, indices = [0], []
+    for i in range(n):
+        indices.extend(range(i))
+        offsets.append(len(indices))
+    return {"n": n, "buffer_size": 2 * (n + 1), "offsets": offsets, "indices": indices}
+
+
+def main(root):
+    data = {
+        "source": "ArborX 2.1.99 test sources (read as text)",
+        "morton": morton_kats(root),
+        "karras": karras_example(root),
+        "assign_morton_codes": assign_morton_codes(root),
+        "degenerate": degenerate_cases(),
+        "crs_query_impl": crs_query_impl(),
+        "stack_capacity": {"cite": "tstQueryTreeDegenerate.cpp:367-446", "n": 4096},
+        "manufactured_grid": {"cite": "tstQueryTreeManufacturedSolution.cpp:64-269", "nx": 11, "L": 100.0},
+    }
+    out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_kats.json")
+    with open(out, "w") as f:
+        json.dump(data, f, indent=1)
+    print("wrote", out)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,191 @@
+"""Pin the CPU oracle to the reference's own known-answer tests.
+
+Every case comes from tests/golden/reference_kats.json (generated from the
+reference's Boost.Test sources by tests/golden/make_golden.py) or restates a
+reference test's construction (cited per test).  No GPU needed.
+"""
+
+import numpy as np
+import pytest
+
+from oracle import oracle as o
+from tests.helpers import assert_crs_multiset_equal, box_list, manufactured_grid, uniform_points
+
+
+def test_expand_bits_kats(golden):
+    # test/tstDetailsMortonCodes.cpp:22-50
+    for case in golden["morton"]["expand_bits32"]:
+        assert o.expand_bits32(case["input"], case["n_zero"]) == case["expected"], case
+    for case in golden["morton"]["expand_bits64"]:
+        assert o.expand_bits64(case["input"], case["n_zero"]) == case["expected"], case
+
+
+def test_morton_kats(golden):
+    # test/tstDetailsMortonCodes.cpp:52-82 (1D, 2D and 3D points)
+    for case in golden["morton"]["morton"]:
+        f = o.morton32 if case["bits"] == 32 else o.morton64
+        assert f(case["point"]) == case["expected"], case
+
+
+def test_assign_morton_codes(golden):
+    # test/tstDetailsTreeConstruction.cpp:33-102: boxes around 7 points
+    c = golden["assign_morton_codes"]
+    pts = np.asarray(c["points"], np.float32)
+    boxes = np.concatenate([pts, pts], axis=1)
+    scene = o.scene_bounds(boxes, is_box=True)
+    assert scene.tolist() == np.asarray(c["scene"], np.float32).tolist()
+    codes = o.morton64_codes(boxes, scene, is_box=True)
+    e = lambda v: o.expand_bits64(v, 2)  # noqa: E731
+    ref = [4 * e(i) + 2 * e(j) + e(k) for i, j, k in c["anchors"]]
+    assert codes.tolist() == ref
+
+
+def test_indirect_sort():
+    # test/tstDetailsTreeConstruction.cpp:119-149
+    keys, perm = o.sort_u32([4, 3, 2, 1])
+    assert keys.tolist() == [1, 2, 3, 4]
+    assert perm.tolist() == [3, 2, 1, 0]
+    keys, perm = o.sort_u64([4, 3, 2, 1])
+    assert perm.tolist() == [3, 2, 1, 0]
+
+
+def test_sort_is_stable():
+    rng = np.random.default_rng(5)
+    keys = rng.integers(0, 7, 1000).astype(np.uint64)
+    _, perm = o.sort_u64(keys)
+    assert np.array_equal(perm, np.argsort(keys, kind="stable"))
+
+
+def _dfs_string(leaves, internal, n):
+    out = []
+    node = n
+
+    def walk(node):
+        if node < n:
+            out.append("L%d" % node)
+            if leaves[node]["rope"] != -1:
+                walk(int(leaves[node]["rope"]))
+        else:
+            out.append("I%d" % (node - n))
+            walk(int(internal[node - n]["left_child"]))
+
+    walk(node)
+    return "".join(out)
+
+
+def test_karras_example(golden):
+    # test/tstDetailsTreeConstruction.cpp:217-269: exact rope / left-child
+    # depth-first order for the 8-key example of Karras
+    codes = np.asarray(golden["karras"]["sorted_codes"], np.uint64)
+    n = codes.size
+    geom = np.zeros((n, 3), np.float32)
+    leaves, internal = o.generate_hierarchy(geom, np.arange(n, dtype=np.uint32), codes)
+    assert _dfs_string(leaves, internal, n) == golden["karras"]["dfs"]
+
+
+def _run_case(case):
+    leaves = box_list(case["leaves"])
+    tree = o.OracleTree(leaves, is_box=True)
+    if case["kind"] == "nearest":
+        q = np.asarray(case["queries"], np.float32).reshape(-1, 4)
+        res = []
+        for mode in (o.MODE_ARBORX, o.MODE_ORDERED):
+            off, ind, _ = tree.nearest(q[:, :3], q[:, 3].astype(np.int32), mode=mode)
+            res.append((off, ind))
+        return res
+    kind = o.KIND_BOX if case["kind"] == "box" else o.KIND_SPHERE
+    q = box_list(case["queries"]) if kind == o.KIND_BOX else np.asarray(case["queries"], np.float32).reshape(-1, 4)
+    return [tree.spatial(kind, q)]
+
+
+def test_degenerate_and_policy_cases(golden):
+    # test/tstQueryTreeDegenerate.cpp:25-361, tstQueryTreeTraversalPolicy.cpp
+    for case in golden["degenerate"]:
+        for off, ind in _run_case(case):
+            assert_crs_multiset_equal(off, ind, case["offsets"], case["indices"])
+
+
+def test_tree_bounds_degenerate():
+    # empty tree bounds = default box; single leaf bounds = the leaf
+    t = o.OracleTree(np.zeros((0, 6), np.float32), is_box=True)
+    assert t.bounds.tolist() == box_list(["empty"])[0].tolist()
+    t = o.OracleTree(np.asarray([[0, 0, 0, 1, 1, 1]], np.float32), is_box=True)
+    assert t.bounds.tolist() == [0, 0, 0, 1, 1, 1]
+
+
+def test_manufactured_grid():
+    # test/tstQueryTreeManufacturedSolution.cpp:29-270
+    leaves, cases = manufactured_grid()
+    tree = o.OracleTree(leaves, is_box=True)
+    for q, (eoff, eind) in cases:
+        off, ind = tree.spatial(o.KIND_BOX, q)
+        assert_crs_multiset_equal(off, ind, eoff, eind)
+
+
+def test_stack_capacity():
+    # test/tstQueryTreeDegenerate.cpp:367-446: 4096 unit boxes on the
+    # diagonal, a query touching all of them, kNN with k = n
+    n = 4096
+    a = np.arange(n, dtype=np.float32)
+    boxes = np.stack([a, a, a, a + 1, a + 1, a + 1], axis=1)
+    tree = o.OracleTree(boxes, is_box=True)
+    q = box_list(["empty", [0, 0, 0, n, n, n]])
+    off, _ = tree.spatial(o.KIND_BOX, q)
+    assert off[-1] == n
+    for mode in (o.MODE_ARBORX, o.MODE_ORDERED):
+        off, ind, _ = tree.nearest(np.zeros((1, 3), np.float32), n, mode=mode)
+        assert off[-1] == n and sorted(ind.tolist()) == list(range(n))
+
+
+@pytest.mark.parametrize("n,nq,k", [(1000, 300, 1), (5000, 500, 10), (20000, 300, 16), (3, 10, 5)])
+def test_oracle_knn_matches_brute_force(n, nq, k):
+    p = uniform_points(n, 1)
+    q = uniform_points(nq, 2)
+    tree = o.OracleTree(p)
+    off, ind, dist = tree.nearest(q, k)
+    bi, bd = o.knn_brute(p, q, k)
+    kk = min(k, n)
+    assert np.array_equal(off, np.arange(nq + 1) * kk)
+    assert np.array_equal(ind.reshape(nq, kk), bi)
+    assert np.array_equal(dist.reshape(nq, kk), bd)
+    # verbatim ArborX rule: same distances, sets equal up to ties at the k-th
+    off2, ind2, dist2 = tree.nearest(q, k, mode=o.MODE_ARBORX)
+    assert np.array_equal(np.sort(dist2.reshape(nq, kk), axis=1), bd)
+
+
+def test_oracle_knn_fp64_check():
+    # every float32 distance is the correctly rounded chain of the formula;
+    # against float64 it is within a few ulps
+    p = uniform_points(4000, 3)
+    q = uniform_points(200, 4)
+    tree = o.OracleTree(p)
+    off, ind, dist = tree.nearest(q, 8)
+    d64 = np.sqrt(((p[ind].astype(np.float64) - np.repeat(q, 8, axis=0).astype(np.float64)) ** 2).sum(1))
+    assert np.all(np.abs(dist - d64) <= 4 * np.spacing(dist.astype(np.float32)).astype(np.float64) + 1e-12)
+
+
+@pytest.mark.parametrize("kind", [o.KIND_SPHERE, o.KIND_BOX])
+def test_oracle_spatial_matches_brute_force(kind):
+    p = uniform_points(20000, 5)
+    c = uniform_points(500, 6)
+    if kind == o.KIND_SPHERE:
+        preds = np.concatenate([c, np.full((500, 1), 0.05, np.float32)], axis=1)
+    else:
+        preds = np.concatenate([c - 0.04, c + 0.04], axis=1).astype(np.float32)
+    tree = o.OracleTree(p)
+    off, ind = tree.spatial(kind, preds)
+    boff, bind = o.spatial_brute(p, kind, preds)
+    assert_crs_multiset_equal(off, ind, boff, bind)
+
+
+def test_oracle_duplicates_and_line():
+    # adversarial inputs: all-equal points and points on a line
+    same = np.ones((257, 3), np.float32)
+    line = np.repeat(np.linspace(0, 1, 300, dtype=np.float32)[:, None], 3, axis=1)
+    for p in (same, line):
+        tree = o.OracleTree(p)
+        q = uniform_points(50, 7)
+        off, ind, dist = tree.nearest(q, 7)
+        bi, bd = o.knn_brute(p, q, 7)
+        assert np.array_equal(ind.reshape(-1, 7), bi)
+        assert np.array_equal(dist.reshape(-1, 7), bd)
