@@ -1,0 +1,118 @@
+"""ctypes binding of libarborx_gb300.so (the C ABI of include/arborx_gb300.h).
+
+Loading fails loudly when the library has not been built: there is no CPU
+fallback anywhere in this package.
+"""
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libarborx_gb300.so")
+
+# abx_status
+SUCCESS = 0
+ERROR_INVALID_ARGUMENT = 1
+ERROR_CUDA = 2
+ERROR_OUT_OF_MEMORY = 3
+ERROR_BUFFER_OVERFLOW = 4
+ERROR_DEVICE = 5
+ERROR_NOT_SUPPORTED = 6
+ERROR_TIMEOUT = 7
+
+# abx_geometry
+POINT, BOX, SPHERE = 0, 1, 2
+
+# Every function the header declares: name -> (restype, argtypes)
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_I32 = ctypes.c_int32
+_STATUS = ctypes.c_int
+
+
+class TraversalPolicyC(ctypes.Structure):
+    _fields_ = [("buffer_size", ctypes.c_int32), ("sort_predicates", ctypes.c_int32)]
+
+
+SIGNATURES = {
+    "abx_status_string": (ctypes.c_char_p, [_STATUS]),
+    "abx_last_error": (ctypes.c_char_p, []),
+    "abx_version": (ctypes.c_char_p, []),
+    "abx_device_errors": (_STATUS, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    "abx_profiling_enable": (_STATUS, [_I32]),
+    "abx_profiling_stage": (_STATUS, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)]),
+    "abx_profiling_reset": (_STATUS, []),
+    "abx_bvh_create": (_STATUS, [_P, ctypes.c_int, _P, _I64, ctypes.POINTER(_P)]),
+    "abx_bvh_destroy": (_STATUS, [_P]),
+    "abx_bvh_size": (_I64, [_P]),
+    "abx_bvh_bounds": (_STATUS, [_P, _P]),
+    "abx_bvh_geometry": (ctypes.c_int, [_P]),
+    "abx_bvh_export_nodes": (_STATUS, [_P, _P, _P, _P]),
+    "abx_bvh_query_intersects": (
+        _STATUS,
+        [_P, _P, ctypes.c_int, _P, _I64, TraversalPolicyC, ctypes.POINTER(_P)],
+    ),
+    "abx_bvh_query_nearest": (
+        _STATUS,
+        [_P, _P, _P, _I64, _P, _I32, TraversalPolicyC, _I32, ctypes.POINTER(_P)],
+    ),
+    "abx_crs_num_queries": (_I64, [_P]),
+    "abx_crs_num_results": (_I64, [_P]),
+    "abx_crs_offsets": (_P, [_P]),
+    "abx_crs_indices": (_P, [_P]),
+    "abx_crs_distances": (_P, [_P]),
+    "abx_crs_destroy": (_STATUS, [_P]),
+    "abx_scene_bounds": (_STATUS, [_P, ctypes.c_int, _P, _I64, _P]),
+    "abx_morton64": (_STATUS, [_P, ctypes.c_int, _P, _I64, _P, _P]),
+    "abx_morton32": (_STATUS, [_P, ctypes.c_int, _P, _I64, _P, _P]),
+    "abx_sort_u64": (_STATUS, [_P, _P, _I64, _P]),
+    "abx_sort_u32": (_STATUS, [_P, _P, _I64, _P]),
+    "abx_generate_hierarchy": (_STATUS, [_P, ctypes.c_int, _P, _I64, _P, _P, _P, _P]),
+    "abx_exclusive_scan_i32": (_STATUS, [_P, _P, _I64, _P]),
+}
+
+
+class AbxError(RuntimeError):
+    """A failing call of the C ABI (status + the library's message)."""
+
+    def __init__(self, status, message):
+        super().__init__(message)
+        self.status = status
+
+
+class SearchException(AbxError):
+    """Mirror of ArborX::SearchException (src/misc/ArborX_Exception.hpp:19-37),
+    raised for ABX_ERROR_BUFFER_OVERFLOW and invalid arguments."""
+
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the shared library; raises ImportError if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(
+            "libarborx_gb300.so is not built (expected at %s); run "
+            "`python -c 'import arborx_gb300.build as b; b.build()'`" % path
+        )
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status):
+    if status == SUCCESS:
+        return
+    L = load()
+    name = L.abx_status_string(status).decode()
+    msg = "%s: %s" % (name, L.abx_last_error().decode())
+    if status in (ERROR_BUFFER_OVERFLOW, ERROR_INVALID_ARGUMENT):
+        raise SearchException(status, msg)
+    raise AbxError(status, msg)

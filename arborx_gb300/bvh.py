@@ -1,0 +1,321 @@
+"""Python mirror of the ArborX BVH interface over the C ABI.
+
+Mirrors (reference paths relative to the ArborX source tree):
+  BoundingVolumeHierarchy   src/spatial/ArborX_LinearBVH.hpp:57-142
+  query(tree, preds, ...)   src/spatial/ArborX_CrsGraphWrapper.hpp:22-34
+  intersects / nearest      src/spatial/detail/ArborX_Predicates.hpp:57-142
+  make_intersects/_nearest  src/spatial/detail/ArborX_PredicateHelpers.hpp:92-206
+  TraversalPolicy           src/spatial/detail/ArborX_TraversalPolicy.hpp:19-47
+Tensors are torch CUDA tensors (PyTorch is only the device-memory and stream
+plumbing); every computation is a kernel of libarborx_gb300.so.
+"""
+
+import ctypes
+
+import torch
+
+from . import _lib
+from ._lib import BOX, POINT, SPHERE, TraversalPolicyC, check
+
+
+def version():
+    return _lib.load().abx_version().decode()
+
+
+def _stream(space):
+    if space is None:
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(space, torch.cuda.Stream):
+        return ctypes.c_void_p(space.cuda_stream)
+    return ctypes.c_void_p(int(space))
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else ctypes.c_void_p(0)
+
+
+def _as_rows(t, cols, name):
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("%s must be a CUDA tensor" % name)
+    if t.dtype != torch.float32:
+        t = t.to(torch.float32)
+    t = t.contiguous()
+    if t.numel() % cols != 0:
+        raise ValueError("%s: expected rows of %d floats, got shape %s" % (name, cols, tuple(t.shape)))
+    return t.view(-1, cols)
+
+
+class _CrsOwner:
+    """Owns an abx_crs; freed when the last view of its arrays goes away."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    def __del__(self):
+        if self.handle:
+            try:
+                _lib.load().abx_crs_destroy(self.handle)
+            except Exception:  # interpreter shutdown
+                pass
+            self.handle = None
+
+
+class _DeviceArray:
+    def __init__(self, owner, ptr, n, typestr):
+        self._owner = owner
+        self.__cuda_array_interface__ = {
+            "shape": (int(n),),
+            "typestr": typestr,
+            "data": (int(ptr), False),
+            "version": 2,
+        }
+
+
+def _view(owner, ptr, n, dtype):
+    if n == 0 or not ptr:
+        return torch.empty(0, dtype=dtype, device="cuda")
+    typestr = {torch.int32: "<i4", torch.float32: "<f4"}[dtype]
+    return torch.as_tensor(_DeviceArray(owner, ptr, n, typestr), device="cuda")
+
+
+class TraversalPolicy:
+    """ArborX::Experimental::TraversalPolicy: buffer size 0 (two-pass), > 0
+    (single pass, second pass on overflow), < 0 (single pass, overflow raises
+    SearchException); predicate sorting on by default."""
+
+    def __init__(self, buffer_size=0, sort_predicates=True):
+        self._buffer_size = int(buffer_size)
+        self._sort_predicates = bool(sort_predicates)
+
+    def setBufferSize(self, buffer_size):  # noqa: N802 (ArborX spelling)
+        self._buffer_size = int(buffer_size)
+        return self
+
+    def setPredicateSorting(self, sort_predicates):  # noqa: N802
+        self._sort_predicates = bool(sort_predicates)
+        return self
+
+    def _c(self):
+        return TraversalPolicyC(self._buffer_size, 1 if self._sort_predicates else 0)
+
+
+class Intersects:
+    """Batch of intersects(geometry) predicates: spheres [nq,4] (cx cy cz r)
+    or boxes [nq,6] (min xyz, max xyz)."""
+
+    def __init__(self, geometry, kind):
+        self.kind = kind
+        self.data = _as_rows(geometry, 4 if kind == SPHERE else 6, "intersects geometry")
+
+    def __len__(self):
+        return self.data.shape[0]
+
+
+class Nearest:
+    """Batch of nearest(point, k) predicates: points [nq,3] and k (int or an
+    int32 CUDA tensor with one k per query)."""
+
+    def __init__(self, points, k=1):
+        self.data = _as_rows(points, 3, "nearest points")
+        if isinstance(k, torch.Tensor):
+            self.k = k.to(device=self.data.device, dtype=torch.int32).contiguous()
+        else:
+            self.k = int(k)
+
+    def __len__(self):
+        return self.data.shape[0]
+
+
+def intersects(geometry, kind=None):
+    g = geometry
+    if kind is None:
+        cols = g.shape[-1]
+        kind = {4: SPHERE, 6: BOX}.get(cols)
+        if kind is None:
+            raise ValueError("intersects: geometry must have 4 (sphere) or 6 (box) columns")
+    return Intersects(g, kind)
+
+
+def nearest(points, k=1):
+    return Nearest(points, k)
+
+
+def make_intersects(points, r):
+    """intersects(Sphere{p, r}) for every point (ArborX_PredicateHelpers.hpp:99-105)."""
+    p = _as_rows(points, 3, "points")
+    rr = torch.full((p.shape[0], 1), float(r), dtype=torch.float32, device=p.device)
+    return Intersects(torch.cat([p, rr], dim=1), SPHERE)
+
+
+def make_nearest(points, k):
+    """nearest(p, k) for every point (ArborX_PredicateHelpers.hpp:114-119)."""
+    return Nearest(points, k)
+
+
+class BoundingVolumeHierarchy:
+    """Tree over points [n,3] or boxes [n,6]; the value of each leaf is its
+    row index (ArborX's benchmark form BVH<MemorySpace, int, ...>)."""
+
+    def __init__(self, values=None, space=None, kind=None):
+        L = _lib.load()
+        self._h = ctypes.c_void_p()
+        if values is None:
+            values = torch.empty((0, 3), dtype=torch.float32, device="cuda")
+            kind = POINT
+        if kind is None:
+            kind = {3: POINT, 6: BOX}.get(values.shape[-1])
+            if kind is None:
+                raise ValueError("values must have 3 (point) or 6 (box) columns")
+        self.kind = kind
+        v = _as_rows(values, 3 if kind == POINT else 6, "values")
+        self._stream = _stream(space)
+        check(L.abx_bvh_create(self._stream, kind, _ptr(v), v.shape[0], ctypes.byref(self._h)))
+        self._values = v  # kept until the build has consumed it
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.load().abx_bvh_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def size(self):
+        return int(_lib.load().abx_bvh_size(self._h))
+
+    def empty(self):
+        return self.size() == 0
+
+    def bounds(self):
+        """The root box as (min xyz, max xyz); waits for the build."""
+        out = (ctypes.c_float * 6)()
+        check(_lib.load().abx_bvh_bounds(self._h, out))
+        return tuple(out)
+
+    def export_nodes(self, space=None):
+        """Node arrays in the reference layout: leaves int32 [n,2] (rope,
+        value) and internal nodes int32 [n-1,8] (left_child, rope, then the
+        box's 6 floats stored bit-for-bit)."""
+        n = self.size()
+        leaves = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+        internal = torch.empty((max(n - 1, 0), 8), dtype=torch.int32, device="cuda")
+        check(_lib.load().abx_bvh_export_nodes(self._h, _stream(space), _ptr(leaves), _ptr(internal)))
+        return leaves, internal
+
+    def query(self, predicates, policy=None, space=None, with_distances=False):
+        return query(self, predicates, policy, space=space, with_distances=with_distances)
+
+
+BVH = BoundingVolumeHierarchy
+
+
+def query(tree, predicates, policy=None, space=None, with_distances=False):
+    """ArborX::query(tree, space, predicates, indices, offsets[, policy]).
+
+    Returns (indices, offsets) as int32 CUDA tensors; nearest predicates with
+    with_distances=True also return the float32 distances."""
+    L = _lib.load()
+    policy = policy or TraversalPolicy()
+    s = _stream(space)
+    h = ctypes.c_void_p()
+    if isinstance(predicates, Intersects):
+        check(
+            L.abx_bvh_query_intersects(
+                tree._h, s, predicates.kind, _ptr(predicates.data), len(predicates), policy._c(),
+                ctypes.byref(h),
+            )
+        )
+    elif isinstance(predicates, Nearest):
+        kt = predicates.k if isinstance(predicates.k, torch.Tensor) else None
+        kv = 0 if kt is not None else predicates.k
+        check(
+            L.abx_bvh_query_nearest(
+                tree._h, s, _ptr(predicates.data), len(predicates), _ptr(kt) if kt is not None else None,
+                kv, policy._c(), 1 if with_distances else 0, ctypes.byref(h),
+            )
+        )
+    else:
+        raise TypeError("predicates must be Intersects or Nearest")
+    owner = _CrsOwner(h)
+    nq = L.abx_crs_num_queries(h)
+    nres = L.abx_crs_num_results(h)
+    offsets = _view(owner, L.abx_crs_offsets(h), nq + 1, torch.int32)
+    indices = _view(owner, L.abx_crs_indices(h), nres, torch.int32)
+    if isinstance(predicates, Nearest) and with_distances:
+        dist = _view(owner, L.abx_crs_distances(h), nres, torch.float32)
+        return indices, offsets, dist
+    return indices, offsets
+
+
+# ---------------------------------------------------------------------------
+# Building blocks (the reference's Details functions)
+# ---------------------------------------------------------------------------
+
+
+def device_errors(space=None):
+    bits = ctypes.c_uint32(0)
+    check(_lib.load().abx_device_errors(_stream(space), ctypes.byref(bits)))
+    return bits.value
+
+
+def scene_bounds(values, kind=POINT, space=None):
+    v = _as_rows(values, 3 if kind == POINT else 6, "values")
+    out = torch.empty(6, dtype=torch.float32, device="cuda")
+    check(_lib.load().abx_scene_bounds(_stream(space), kind, _ptr(v), v.shape[0], _ptr(out)))
+    return out
+
+
+def morton64(values, scene, kind=POINT, space=None):
+    """Morton64 codes (uint64 bit patterns in an int64 tensor)."""
+    v = _as_rows(values, {POINT: 3, BOX: 6, SPHERE: 4}[kind], "values")
+    sc = scene.to(device="cuda", dtype=torch.float32).contiguous()
+    out = torch.empty(v.shape[0], dtype=torch.int64, device="cuda")
+    check(_lib.load().abx_morton64(_stream(space), kind, _ptr(v), v.shape[0], _ptr(sc), _ptr(out)))
+    return out
+
+
+def morton32(values, scene, kind=POINT, space=None):
+    """Morton32 codes (uint32 bit patterns in an int32 tensor)."""
+    v = _as_rows(values, {POINT: 3, BOX: 6, SPHERE: 4}[kind], "values")
+    sc = scene.to(device="cuda", dtype=torch.float32).contiguous()
+    out = torch.empty(v.shape[0], dtype=torch.int32, device="cuda")
+    check(_lib.load().abx_morton32(_stream(space), kind, _ptr(v), v.shape[0], _ptr(sc), _ptr(out)))
+    return out
+
+
+def sort_u64(keys, space=None):
+    """Stable sort of uint64 keys (int64 tensor, sorted in place); returns the
+    permutation (int32 tensor)."""
+    assert keys.dtype == torch.int64 and keys.is_cuda and keys.is_contiguous()
+    perm = torch.empty(keys.numel(), dtype=torch.int32, device="cuda")
+    check(_lib.load().abx_sort_u64(_stream(space), _ptr(keys), keys.numel(), _ptr(perm)))
+    return perm
+
+
+def sort_u32(keys, space=None):
+    assert keys.dtype == torch.int32 and keys.is_cuda and keys.is_contiguous()
+    perm = torch.empty(keys.numel(), dtype=torch.int32, device="cuda")
+    check(_lib.load().abx_sort_u32(_stream(space), _ptr(keys), keys.numel(), _ptr(perm)))
+    return perm
+
+
+def generate_hierarchy(values, permutation, sorted_codes, kind=POINT, space=None):
+    v = _as_rows(values, 3 if kind == POINT else 6, "values")
+    n = v.shape[0]
+    leaves = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+    internal = torch.empty((max(n - 1, 0), 8), dtype=torch.int32, device="cuda")
+    check(
+        _lib.load().abx_generate_hierarchy(
+            _stream(space), kind, _ptr(v), n, _ptr(permutation.contiguous()),
+            _ptr(sorted_codes.contiguous()), _ptr(leaves), _ptr(internal),
+        )
+    )
+    return leaves, internal
+
+
+def exclusive_scan(values, space=None):
+    v = values.to(torch.int32).contiguous()
+    out = torch.empty(v.numel() + 1, dtype=torch.int32, device="cuda")
+    check(_lib.load().abx_exclusive_scan_i32(_stream(space), _ptr(v), v.numel(), _ptr(out)))
+    return out

@@ -1,0 +1,64 @@
+// abx_build.h -- host launchers of the construction and query kernels.
+#pragma once
+
+#include "abx_common.cuh"
+#include "abx_internal.h"
+
+namespace abx
+{
+
+abx_status scene_bounds(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
+                        float *d_out);
+
+// d_hist (optional, zeroed, 8 x 256) receives the radix digit histograms.
+abx_status morton64_codes(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
+                          const float *d_scene, uint64_t *d_codes, uint32_t *d_hist);
+
+// d_hist (optional, zeroed, 4 x 256).
+abx_status morton32_codes(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
+                          const float *d_scene, uint32_t *d_codes, uint32_t *d_hist);
+
+// n >= 2.  d_tnodes may be null (then only the reference layout is written).
+abx_status generate_hierarchy(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
+                              const uint32_t *d_perm, const uint64_t *d_codes,
+                              LeafNode *d_leaves, InternalNode *d_internal, TNode *d_tnodes);
+
+abx_status single_leaf(cudaStream_t s, abx_geometry kind, const float *d_g,
+                       LeafNode *d_leaves, TNode *d_tnodes, float *d_bounds);
+
+// Tree view used by the query launchers.
+struct TreeView
+{
+  const TNode *tnodes;
+  int64_t n;
+  const float *d_bounds; // 6 floats, the tree bounds
+};
+
+// Spatial query modes.
+enum SpatialMode
+{
+  kCount = 0,  // counts[q] = number of hits
+  kFill = 1,   // out[offsets[q] + j] = j-th hit
+  kBuffered = 2 // out[q * buffer + j] for j < buffer, counts[q] = hits
+};
+
+abx_status launch_spatial(cudaStream_t s, TreeView const &t, abx_geometry pred_kind,
+                          const float *d_preds, int64_t nq, const uint32_t *d_perm,
+                          SpatialMode mode, int32_t *d_counts, const int32_t *d_offsets,
+                          int32_t *d_out, int32_t buffer, unsigned *d_overflow);
+
+abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int32_t buffer,
+                          const int32_t *d_offsets, int32_t *d_out);
+
+// kNN: d_offsets null means uniform k (offset q * min(k, n)), and then
+// d_offsets_out (nq + 1) is filled by the kernel.  max_k bounds every k.
+abx_status launch_nearest(cudaStream_t s, TreeView const &t, const float *d_queries,
+                          int64_t nq, const uint32_t *d_perm, const int32_t *d_k,
+                          int32_t k, int32_t max_k, const int32_t *d_offsets,
+                          int32_t *d_offsets_out, int32_t *d_idx, float *d_dist);
+
+// counts[q] = min(max(k_q, 0), n), max over queries into *d_max (zeroed).
+abx_status launch_knn_counts(cudaStream_t s, const int32_t *d_k, int64_t nq, int64_t n,
+                             int32_t *d_counts, int32_t *d_max);
+
+} // namespace abx

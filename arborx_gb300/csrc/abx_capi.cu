@@ -1,0 +1,716 @@
+// abx_capi.cu -- the extern "C" entry points of include/arborx_gb300.h:
+// tree construction pipeline, CRS query drivers, result objects, per-device
+// state and error reporting.
+#include <atomic>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "abx_build.h"
+
+// ---------------------------------------------------------------------------
+// Opaque objects
+// ---------------------------------------------------------------------------
+
+struct abx_bvh
+{
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  abx_geometry kind = ABX_POINT;
+  int64_t n = 0;
+  abx::LeafNode *leaves = nullptr;
+  abx::InternalNode *internal = nullptr;
+  abx::TNode *tnodes = nullptr;
+  float *d_bounds = nullptr; // tree bounds on the device (6 floats)
+  float *h_bounds = nullptr; // pinned copy, valid once `ready` completed
+  cudaEvent_t ready = nullptr;
+};
+
+struct abx_crs
+{
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int64_t nq = 0;
+  int64_t nres = 0;
+  int32_t *offsets = nullptr;
+  int32_t *indices = nullptr;
+  float *distances = nullptr;
+};
+
+namespace abx
+{
+
+namespace
+{
+thread_local std::string g_last_error;
+std::mutex g_state_mutex;
+constexpr int kMaxDevices = 64;
+DeviceState g_states[kMaxDevices];
+} // namespace
+
+DeviceState &device_state()
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kMaxDevices)
+    dev = 0;
+  DeviceState &st = g_states[dev];
+  if (st.device >= 0)
+    return st;
+  std::lock_guard<std::mutex> lock(g_state_mutex);
+  if (st.device < 0)
+  {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned *err = nullptr;
+    if (cudaMalloc(&err, sizeof(unsigned)) == cudaSuccess)
+      cudaMemset(err, 0, sizeof(unsigned));
+    // keep freed stream-ordered memory in the pool between calls
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess)
+    {
+      uint64_t threshold = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+    }
+    st.num_sms = sms > 0 ? sms : 1;
+    st.d_error = err;
+    st.device = dev;
+  }
+  return st;
+}
+
+abx_status fail(abx_status status, std::string const &message)
+{
+  g_last_error = message;
+  return status;
+}
+
+abx_status fail_cuda(cudaError_t err, char const *what)
+{
+  cudaGetLastError(); // clear a sticky launch error
+  std::string msg = std::string(what) + ": " + cudaGetErrorName(err) + " (" +
+                    cudaGetErrorString(err) + ")";
+  return fail(err == cudaErrorMemoryAllocation ? ABX_ERROR_OUT_OF_MEMORY : ABX_ERROR_CUDA, msg);
+}
+
+namespace
+{
+struct StageRecord
+{
+  std::string stage;
+  cudaEvent_t start;
+  cudaEvent_t end;
+  int kernels;
+};
+std::mutex g_prof_mutex;
+std::vector<StageRecord> g_prof;
+std::atomic<bool> g_prof_on{false};
+} // namespace
+
+StageScope::StageScope(cudaStream_t s, char const *stage, int kernels)
+    : stream_(s), stage_(stage), kernels_(kernels)
+{
+  if (g_prof_on.load(std::memory_order_relaxed))
+  {
+    if (cudaEventCreate(&start_) == cudaSuccess)
+      cudaEventRecord(start_, s);
+    else
+      start_ = nullptr;
+  }
+}
+
+StageScope::~StageScope()
+{
+  if (!start_)
+    return;
+  cudaEvent_t end;
+  if (cudaEventCreate(&end) != cudaSuccess)
+  {
+    cudaEventDestroy(start_);
+    return;
+  }
+  cudaEventRecord(end, stream_);
+  std::lock_guard<std::mutex> lock(g_prof_mutex);
+  g_prof.push_back(StageRecord{stage_, start_, end, kernels_});
+}
+
+cudaError_t dmalloc(void **p, size_t bytes, cudaStream_t s)
+{
+  return cudaMallocAsync(p, bytes, s);
+}
+
+void dfree(void *p, cudaStream_t s)
+{
+  if (p)
+    cudaFreeAsync(p, s);
+}
+
+} // namespace abx
+
+using namespace abx;
+
+namespace
+{
+
+cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Synchronise the stream and report the device error word (cleared).
+abx_status sync_and_check(cudaStream_t s)
+{
+  ABX_CUDA_TRY(cudaStreamSynchronize(s));
+  DeviceState &ds = device_state();
+  unsigned bits = 0;
+  ABX_CUDA_TRY(cudaMemcpy(&bits, ds.d_error, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  if (bits)
+  {
+    cudaMemset(ds.d_error, 0, sizeof(unsigned));
+    return fail(bits & ABX_DEVERR_TIMEOUT ? ABX_ERROR_TIMEOUT : ABX_ERROR_DEVICE,
+                "device error word 0x" + std::to_string(bits));
+  }
+  return ABX_SUCCESS;
+}
+
+void destroy_tree(abx_bvh *t)
+{
+  if (!t)
+    return;
+  cudaStream_t s = t->stream;
+  dfree(t->leaves, s);
+  dfree(t->internal, s);
+  dfree(t->tnodes, s);
+  dfree(t->d_bounds, s);
+  if (t->h_bounds)
+  {
+    if (t->ready)
+      cudaEventSynchronize(t->ready);
+    cudaFreeHost(t->h_bounds);
+  }
+  if (t->ready)
+    cudaEventDestroy(t->ready);
+  delete t;
+}
+
+void destroy_crs(abx_crs *c)
+{
+  if (!c)
+    return;
+  dfree(c->offsets, c->stream);
+  dfree(c->indices, c->stream);
+  dfree(c->distances, c->stream);
+  delete c;
+}
+
+abx_status build_tree(abx_bvh *t, const float *d_values)
+{
+  cudaStream_t s = t->stream;
+  const int64_t n = t->n;
+  const float empty[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+  std::memcpy(t->h_bounds, empty, sizeof(empty));
+  ABX_CUDA_TRY(dmalloc_n(&t->d_bounds, 6, s));
+  if (n == 0)
+  {
+    ABX_CUDA_TRY(cudaMemcpyAsync(t->d_bounds, empty, sizeof(empty), cudaMemcpyHostToDevice, s));
+    // the copy reads a stack array: finish it before returning
+    ABX_CUDA_TRY(cudaStreamSynchronize(s));
+    return ABX_SUCCESS;
+  }
+  ABX_CUDA_TRY(dmalloc_n(&t->leaves, n, s));
+  if (n == 1)
+  {
+    ABX_CUDA_TRY(dmalloc_n(&t->tnodes, 1, s));
+    ABX_TRY(single_leaf(s, t->kind, d_values, t->leaves, t->tnodes, t->d_bounds));
+  }
+  else
+  {
+    ABX_CUDA_TRY(dmalloc_n(&t->internal, n - 1, s));
+    ABX_CUDA_TRY(dmalloc_n(&t->tnodes, n - 1, s));
+    Scratch<uint64_t> codes;
+    Scratch<uint32_t> perm;
+    Scratch<uint32_t> hist;
+    ABX_CUDA_TRY(codes.alloc(n, s));
+    ABX_CUDA_TRY(perm.alloc(n, s));
+    ABX_CUDA_TRY(hist.alloc(8 * 256, s));
+    ABX_CUDA_TRY(cudaMemsetAsync(hist.ptr, 0, 8 * 256 * sizeof(uint32_t), s));
+    // the scene box equals the root box (min/max are exact), so it is
+    // computed straight into the tree bounds
+    ABX_TRY(scene_bounds(s, t->kind, d_values, n, t->d_bounds));
+    ABX_TRY(morton64_codes(s, t->kind, d_values, n, t->d_bounds, codes.ptr, hist.ptr));
+    ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, n, 8, hist.ptr));
+    ABX_TRY(generate_hierarchy(s, t->kind, d_values, n, perm.ptr, codes.ptr, t->leaves,
+                               t->internal, t->tnodes));
+  }
+  ABX_CUDA_TRY(cudaMemcpyAsync(t->h_bounds, t->d_bounds, 6 * sizeof(float),
+                               cudaMemcpyDeviceToHost, s));
+  return ABX_SUCCESS;
+}
+
+abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
+                           const float *d_preds, int64_t nq, Scratch<uint32_t> &perm)
+{
+  Scratch<uint32_t> codes;
+  Scratch<uint32_t> hist;
+  ABX_CUDA_TRY(codes.alloc(nq, s));
+  ABX_CUDA_TRY(perm.alloc(nq, s));
+  ABX_CUDA_TRY(hist.alloc(4 * 256, s));
+  ABX_CUDA_TRY(cudaMemsetAsync(hist.ptr, 0, 4 * 256 * sizeof(uint32_t), s));
+  ABX_TRY(morton32_codes(s, kind, d_preds, nq, t->d_bounds, codes.ptr, hist.ptr));
+  ABX_TRY(radix_sort_u32(s, codes.ptr, perm.ptr, nullptr, nq, 4, hist.ptr));
+  return ABX_SUCCESS;
+}
+
+TreeView view_of(const abx_bvh *t) { return TreeView{t->tnodes, t->n, t->d_bounds}; }
+
+} // namespace
+
+extern "C" {
+
+const char *abx_status_string(abx_status status)
+{
+  switch (status)
+  {
+  case ABX_SUCCESS: return "ABX_SUCCESS";
+  case ABX_ERROR_INVALID_ARGUMENT: return "ABX_ERROR_INVALID_ARGUMENT";
+  case ABX_ERROR_CUDA: return "ABX_ERROR_CUDA";
+  case ABX_ERROR_OUT_OF_MEMORY: return "ABX_ERROR_OUT_OF_MEMORY";
+  case ABX_ERROR_BUFFER_OVERFLOW: return "ABX_ERROR_BUFFER_OVERFLOW";
+  case ABX_ERROR_DEVICE: return "ABX_ERROR_DEVICE";
+  case ABX_ERROR_NOT_SUPPORTED: return "ABX_ERROR_NOT_SUPPORTED";
+  case ABX_ERROR_TIMEOUT: return "ABX_ERROR_TIMEOUT";
+  }
+  return "ABX_UNKNOWN_STATUS";
+}
+
+const char *abx_last_error(void) { return g_last_error.c_str(); }
+
+const char *abx_version(void) { return "0.1.0"; }
+
+abx_status abx_device_errors(void *stream, uint32_t *h_bits)
+{
+  if (!h_bits)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_device_errors: null output");
+  ABX_CUDA_TRY(cudaStreamSynchronize(as_stream(stream)));
+  DeviceState &ds = device_state();
+  ABX_CUDA_TRY(cudaMemcpy(h_bits, ds.d_error, sizeof(unsigned), cudaMemcpyDeviceToHost));
+  ABX_CUDA_TRY(cudaMemset(ds.d_error, 0, sizeof(unsigned)));
+  return ABX_SUCCESS;
+}
+
+abx_status abx_profiling_enable(int32_t enable)
+{
+  g_prof_on.store(enable != 0);
+  return ABX_SUCCESS;
+}
+
+abx_status abx_profiling_stage(const char *stage, double *h_total_ms, int64_t *h_launches)
+{
+  if (!stage)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_profiling_stage: null stage");
+  const bool all = std::strcmp(stage, "*") == 0;
+  double total = 0;
+  int64_t launches = 0;
+  std::lock_guard<std::mutex> lock(g_prof_mutex);
+  for (auto const &r : g_prof)
+  {
+    if (!all && r.stage != stage)
+      continue;
+    ABX_CUDA_TRY(cudaEventSynchronize(r.end));
+    float ms = 0;
+    ABX_CUDA_TRY(cudaEventElapsedTime(&ms, r.start, r.end));
+    total += ms;
+    launches += r.kernels;
+  }
+  if (h_total_ms)
+    *h_total_ms = total;
+  if (h_launches)
+    *h_launches = launches;
+  return ABX_SUCCESS;
+}
+
+abx_status abx_profiling_reset(void)
+{
+  std::lock_guard<std::mutex> lock(g_prof_mutex);
+  for (auto const &r : g_prof)
+  {
+    cudaEventSynchronize(r.end);
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.end);
+  }
+  g_prof.clear();
+  return ABX_SUCCESS;
+}
+
+abx_status abx_bvh_create(void *stream, abx_geometry kind, const float *d_values, int64_t n,
+                          abx_bvh **out)
+{
+  if (!out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create: null output handle");
+  *out = nullptr;
+  if (kind != ABX_POINT && kind != ABX_BOX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create: values must be points or boxes");
+  if (n < 0 || n >= (int64_t)INT32_MAX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create: size out of range [0, 2^31-1)");
+  if (n > 0 && !d_values)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create: null values");
+  device_state();
+  abx_bvh *t = new (std::nothrow) abx_bvh;
+  if (!t)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_bvh_create: host allocation");
+  cudaGetDevice(&t->device);
+  t->stream = as_stream(stream);
+  t->kind = kind;
+  t->n = n;
+  cudaError_t e = cudaMallocHost(&t->h_bounds, 6 * sizeof(float));
+  if (e != cudaSuccess)
+  {
+    t->h_bounds = nullptr;
+    destroy_tree(t);
+    return fail_cuda(e, "cudaMallocHost");
+  }
+  e = cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming);
+  if (e != cudaSuccess)
+  {
+    t->ready = nullptr;
+    destroy_tree(t);
+    return fail_cuda(e, "cudaEventCreate");
+  }
+  abx_status st = build_tree(t, d_values);
+  if (st == ABX_SUCCESS)
+  {
+    e = cudaEventRecord(t->ready, t->stream);
+    if (e != cudaSuccess)
+      st = fail_cuda(e, "cudaEventRecord");
+  }
+  if (st != ABX_SUCCESS)
+  {
+    cudaStreamSynchronize(t->stream);
+    destroy_tree(t);
+    return st;
+  }
+  *out = t;
+  return ABX_SUCCESS;
+}
+
+abx_status abx_bvh_destroy(abx_bvh *bvh)
+{
+  destroy_tree(bvh);
+  return ABX_SUCCESS;
+}
+
+int64_t abx_bvh_size(const abx_bvh *bvh) { return bvh ? bvh->n : 0; }
+
+abx_geometry abx_bvh_geometry(const abx_bvh *bvh) { return bvh ? bvh->kind : ABX_POINT; }
+
+abx_status abx_bvh_bounds(const abx_bvh *bvh, float h_box[6])
+{
+  if (!bvh || !h_box)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_bounds: null argument");
+  ABX_CUDA_TRY(cudaEventSynchronize(bvh->ready));
+  std::memcpy(h_box, bvh->h_bounds, 6 * sizeof(float));
+  return ABX_SUCCESS;
+}
+
+abx_status abx_bvh_export_nodes(const abx_bvh *bvh, void *stream, int32_t *d_leaves,
+                                void *d_internal)
+{
+  if (!bvh)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_export_nodes: null tree");
+  cudaStream_t s = as_stream(stream);
+  ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+  if (d_leaves && bvh->n > 0)
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_leaves, bvh->leaves, bvh->n * sizeof(LeafNode),
+                                 cudaMemcpyDeviceToDevice, s));
+  if (d_internal && bvh->n > 1)
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_internal, bvh->internal, (bvh->n - 1) * sizeof(InternalNode),
+                                 cudaMemcpyDeviceToDevice, s));
+  return ABX_SUCCESS;
+}
+
+abx_status abx_bvh_query_intersects(const abx_bvh *bvh, void *stream, abx_geometry kind,
+                                    const float *d_predicates, int64_t nq,
+                                    abx_traversal_policy policy, abx_crs **out)
+{
+  if (!bvh || !out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: null argument");
+  *out = nullptr;
+  if (kind != ABX_SPHERE && kind != ABX_BOX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT,
+                "abx_bvh_query_intersects: predicates must be spheres or boxes");
+  if (nq < 0 || nq >= (int64_t)INT32_MAX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: bad number of queries");
+  if (nq > 0 && !d_predicates)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: null predicates");
+  cudaStream_t s = as_stream(stream);
+  device_state();
+  ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+
+  abx_crs *c = new (std::nothrow) abx_crs;
+  if (!c)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
+  cudaGetDevice(&c->device);
+  c->stream = s;
+  c->nq = nq;
+  auto bail = [&](abx_status st) {
+    cudaStreamSynchronize(s);
+    destroy_crs(c);
+    return st;
+  };
+  if (dmalloc_n(&c->offsets, nq + 1, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS offsets"));
+  if (bvh->n == 0 || nq == 0)
+  {
+    cudaMemsetAsync(c->offsets, 0, (nq + 1) * sizeof(int32_t), s);
+    dmalloc_n(&c->indices, 0, s);
+    *out = c;
+    return ABX_SUCCESS;
+  }
+  Scratch<uint32_t> perm;
+  if (policy.sort_predicates && nq > 1)
+  {
+    abx_status st = sort_predicates(s, bvh, kind, d_predicates, nq, perm);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  const TreeView tv = view_of(bvh);
+  const int64_t buffer = policy.buffer_size < 0 ? -(int64_t)policy.buffer_size
+                                                : (int64_t)policy.buffer_size;
+  int32_t total = 0;
+  if (buffer == 0)
+  {
+    abx_status st = launch_spatial(s, tv, kind, d_predicates, nq, perm.ptr, kCount, c->offsets,
+                                   nullptr, nullptr, 0, nullptr);
+    if (st == ABX_SUCCESS)
+      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    cudaMemcpyAsync(&total, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    st = sync_and_check(s);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
+    st = launch_spatial(s, tv, kind, d_predicates, nq, perm.ptr, kFill, nullptr, c->offsets,
+                        c->indices, 0, nullptr);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  else
+  {
+    if (buffer * nq > ((int64_t)1 << 33))
+      return bail(fail(ABX_ERROR_INVALID_ARGUMENT, "buffer_size x queries too large"));
+    Scratch<int32_t> tmp;
+    Scratch<unsigned> flag;
+    if (tmp.alloc((size_t)(buffer * nq), s) != cudaSuccess || flag.alloc(1, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS buffer"));
+    cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), s);
+    abx_status st = launch_spatial(s, tv, kind, d_predicates, nq, perm.ptr, kBuffered,
+                                   c->offsets, nullptr, tmp.ptr, (int32_t)buffer, flag.ptr);
+    if (st == ABX_SUCCESS)
+      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    unsigned overflow = 0;
+    cudaMemcpyAsync(&total, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&overflow, flag.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    st = sync_and_check(s);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    if (overflow && policy.buffer_size < 0)
+      return bail(fail(ABX_ERROR_BUFFER_OVERFLOW,
+                       "buffer_size " + std::to_string(policy.buffer_size) +
+                           " is too small for the results of some query"));
+    if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
+    if (!overflow)
+      st = launch_compact(s, tmp.ptr, nq, (int32_t)buffer, c->offsets, c->indices);
+    else
+      st = launch_spatial(s, tv, kind, d_predicates, nq, perm.ptr, kFill, nullptr, c->offsets,
+                          c->indices, 0, nullptr);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  c->nres = total;
+  *out = c;
+  return ABX_SUCCESS;
+}
+
+abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream, const float *d_queries,
+                                 int64_t nq, const int32_t *d_k, int32_t k,
+                                 abx_traversal_policy policy, int32_t with_distances,
+                                 abx_crs **out)
+{
+  if (!bvh || !out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: null argument");
+  *out = nullptr;
+  if (nq < 0 || nq >= (int64_t)INT32_MAX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: bad number of queries");
+  if (nq > 0 && !d_queries)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: null queries");
+  cudaStream_t s = as_stream(stream);
+  device_state();
+  ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+
+  abx_crs *c = new (std::nothrow) abx_crs;
+  if (!c)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
+  cudaGetDevice(&c->device);
+  c->stream = s;
+  c->nq = nq;
+  auto bail = [&](abx_status st) {
+    cudaStreamSynchronize(s);
+    destroy_crs(c);
+    return st;
+  };
+  if (dmalloc_n(&c->offsets, nq + 1, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS offsets"));
+  const int64_t n = bvh->n;
+  if (n == 0 || nq == 0)
+  {
+    cudaMemsetAsync(c->offsets, 0, (nq + 1) * sizeof(int32_t), s);
+    dmalloc_n(&c->indices, 0, s);
+    if (with_distances)
+      dmalloc_n(&c->distances, 0, s);
+    *out = c;
+    return ABX_SUCCESS;
+  }
+  Scratch<uint32_t> perm;
+  if (policy.sort_predicates && nq > 1)
+  {
+    abx_status st = sort_predicates(s, bvh, ABX_POINT, d_queries, nq, perm);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  const TreeView tv = view_of(bvh);
+  int64_t total = 0;
+  int32_t max_k = k;
+  if (!d_k)
+  {
+    if (k < 0)
+      k = 0;
+    const int64_t kk = std::min<int64_t>(k, n);
+    total = kk * nq;
+    if (total >= (int64_t)INT32_MAX)
+      return bail(fail(ABX_ERROR_INVALID_ARGUMENT, "nearest: more than 2^31-1 results"));
+  }
+  else
+  {
+    Scratch<int32_t> kmax;
+    if (kmax.alloc(1, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "scratch"));
+    cudaMemsetAsync(kmax.ptr, 0, sizeof(int32_t), s);
+    abx_status st = launch_knn_counts(s, d_k, nq, n, c->offsets, kmax.ptr);
+    if (st == ABX_SUCCESS)
+      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    int32_t t32 = 0;
+    cudaMemcpyAsync(&t32, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&max_k, kmax.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    st = sync_and_check(s);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    total = t32;
+  }
+  if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
+  Scratch<float> dist_tmp;
+  float *dist = nullptr;
+  if (with_distances)
+  {
+    if (dmalloc_n(&c->distances, (size_t)total, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS distances"));
+    dist = c->distances;
+  }
+  else if (max_k > 32)
+  {
+    if (dist_tmp.alloc((size_t)total, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "kNN heap"));
+    dist = dist_tmp.ptr;
+  }
+  abx_status st = launch_nearest(s, tv, d_queries, nq, perm.ptr, d_k, k, max_k,
+                                 d_k ? c->offsets : nullptr, d_k ? nullptr : c->offsets,
+                                 c->indices, dist);
+  if (st != ABX_SUCCESS)
+    return bail(st);
+  c->nres = total;
+  *out = c;
+  return ABX_SUCCESS;
+}
+
+int64_t abx_crs_num_queries(const abx_crs *crs) { return crs ? crs->nq : 0; }
+int64_t abx_crs_num_results(const abx_crs *crs) { return crs ? crs->nres : 0; }
+const int32_t *abx_crs_offsets(const abx_crs *crs) { return crs ? crs->offsets : nullptr; }
+const int32_t *abx_crs_indices(const abx_crs *crs) { return crs ? crs->indices : nullptr; }
+const float *abx_crs_distances(const abx_crs *crs) { return crs ? crs->distances : nullptr; }
+
+abx_status abx_crs_destroy(abx_crs *crs)
+{
+  destroy_crs(crs);
+  return ABX_SUCCESS;
+}
+
+abx_status abx_scene_bounds(void *stream, abx_geometry kind, const float *d_values, int64_t n,
+                            float *d_box_out)
+{
+  if (!d_box_out || n < 0 || (n > 0 && !d_values))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_scene_bounds: bad argument");
+  return scene_bounds(as_stream(stream), kind, d_values, n, d_box_out);
+}
+
+abx_status abx_morton64(void *stream, abx_geometry kind, const float *d_values, int64_t n,
+                        const float *d_scene, uint64_t *d_codes)
+{
+  if (n < 0 || (n > 0 && (!d_values || !d_scene || !d_codes)))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_morton64: bad argument");
+  return morton64_codes(as_stream(stream), kind, d_values, n, d_scene, d_codes, nullptr);
+}
+
+abx_status abx_morton32(void *stream, abx_geometry kind, const float *d_values, int64_t n,
+                        const float *d_scene, uint32_t *d_codes)
+{
+  if (n < 0 || (n > 0 && (!d_values || !d_scene || !d_codes)))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_morton32: bad argument");
+  return morton32_codes(as_stream(stream), kind, d_values, n, d_scene, d_codes, nullptr);
+}
+
+abx_status abx_sort_u64(void *stream, uint64_t *d_keys, int64_t n, uint32_t *d_permutation)
+{
+  if (n < 0 || (n > 0 && (!d_keys || !d_permutation)))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_sort_u64: bad argument");
+  device_state();
+  return radix_sort_u64(as_stream(stream), d_keys, d_permutation, nullptr, n, 8, nullptr);
+}
+
+abx_status abx_sort_u32(void *stream, uint32_t *d_keys, int64_t n, uint32_t *d_permutation)
+{
+  if (n < 0 || (n > 0 && (!d_keys || !d_permutation)))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_sort_u32: bad argument");
+  device_state();
+  return radix_sort_u32(as_stream(stream), d_keys, d_permutation, nullptr, n, 4, nullptr);
+}
+
+abx_status abx_generate_hierarchy(void *stream, abx_geometry kind, const float *d_values,
+                                  int64_t n, const uint32_t *d_permutation,
+                                  const uint64_t *d_sorted_codes, int32_t *d_leaves,
+                                  void *d_internal)
+{
+  if (n < 2 || !d_values || !d_permutation || !d_sorted_codes || !d_leaves || !d_internal)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_generate_hierarchy: bad argument");
+  if (kind != ABX_POINT && kind != ABX_BOX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_generate_hierarchy: points or boxes");
+  device_state();
+  return generate_hierarchy(as_stream(stream), kind, d_values, n, d_permutation, d_sorted_codes,
+                            reinterpret_cast<LeafNode *>(d_leaves),
+                            reinterpret_cast<InternalNode *>(d_internal), nullptr);
+}
+
+abx_status abx_exclusive_scan_i32(void *stream, const int32_t *d_in, int64_t n, int32_t *d_out)
+{
+  if (n < 0 || !d_out || (n > 0 && !d_in))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_exclusive_scan_i32: bad argument");
+  device_state();
+  return exclusive_scan_i32(as_stream(stream), d_in, n, d_out);
+}
+
+} // extern "C"

@@ -1,0 +1,531 @@
+// abx_sort.cu -- stable LSD radix sort of (key, uint32 value) pairs, one
+// onesweep pass per 8-bit digit (decoupled look-back over per-digit tile
+// prefixes), plus the digit histogram and small scan kernels.
+//
+// Replaces sortByKey / sortObjects (src/kokkos_ext/ArborX_KokkosExtSort.hpp:
+// 79-148, src/misc/ArborX_SortUtils.hpp:28-39), which call thrust::sort_by_key
+// on CUDA.  The order of equal keys is fixed here: stable (input order).
+//
+// Pass structure (per tile of 4096 keys, one CTA of 256 threads):
+//   1. load 16 keys per thread in warp-striped order (coalesced);
+//   2. rank every key among the equal digits of its warp with match_any,
+//      keeping a per-warp 256-bin histogram in shared memory;
+//   3. turn the warp histograms into per-digit tile offsets;
+//   4. publish the tile's 256 digit counts, look back over earlier tiles to
+//      get each digit's exclusive prefix (bounded spin, error word on
+//      timeout), publish the inclusive prefix;
+//   5. scatter the tile into shared memory in digit order, then write it out
+//      so that equal-digit runs land on consecutive global addresses.
+#include <algorithm>
+
+#include "abx_common.cuh"
+#include "abx_internal.h"
+
+namespace abx
+{
+namespace
+{
+
+constexpr int kBins = 256;
+constexpr int kSortThreads = 256;
+constexpr int kSortWarps = kSortThreads / 32;
+constexpr int kItems = 16;
+constexpr int kTile = kSortThreads * kItems;
+constexpr int kMaxPasses = 8;
+constexpr int kSpinLimit = 1 << 22;
+
+template <class K>
+__device__ __forceinline__ unsigned digit_of(K key, int shift)
+{
+  return (unsigned)(key >> shift) & 0xffu;
+}
+
+// Per-pass digit histograms of all keys (hist: passes x 256, zeroed).
+template <class K>
+__global__ void __launch_bounds__(256) k_histogram(const K *__restrict__ keys, int64_t n,
+                                                   int num_passes,
+                                                   uint32_t *__restrict__ hist)
+{
+  __shared__ uint32_t sh[kMaxPasses * kBins];
+  for (int i = threadIdx.x; i < num_passes * kBins; i += blockDim.x)
+    sh[i] = 0;
+  __syncthreads();
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+  {
+    K k = keys[i];
+    for (int p = 0; p < num_passes; ++p)
+      atomicAdd(&sh[p * kBins + digit_of(k, 8 * p)], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < num_passes * kBins; i += blockDim.x)
+    if (sh[i])
+      atomicAdd(&hist[i], sh[i]);
+}
+
+// offsets[p][d] = sum of hist[p][d'] for d' < d.  One CTA of 256 per pass.
+__global__ void __launch_bounds__(256) k_hist_scan(const uint32_t *__restrict__ hist,
+                                                   uint32_t *__restrict__ offsets)
+{
+  __shared__ uint32_t warp_sums[kSortWarps];
+  int t = threadIdx.x;
+  uint32_t v = hist[blockIdx.x * kBins + t];
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if ((t & 31) >= o)
+      x += y;
+  }
+  if ((t & 31) == 31)
+    warp_sums[t >> 5] = x;
+  __syncthreads();
+  uint32_t pre = 0;
+  for (int w = 0; w < (t >> 5); ++w)
+    pre += warp_sums[w];
+  offsets[blockIdx.x * kBins + t] = pre + x - v;
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p)
+{
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long *p, unsigned long long v)
+{
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+template <class K>
+struct PassSmem
+{
+  union
+  {
+    uint32_t whist[kSortWarps][kBins + 1];
+    struct
+    {
+      K keys[kTile];
+      uint32_t vals[kTile];
+    } exch;
+  } u;
+  uint32_t digit_start[kBins + 1];
+  uint32_t gbase[kBins];
+  uint32_t warp_tot[kSortWarps];
+  uint32_t tile;
+};
+
+// One onesweep pass.  Look-back words: (tag << 32) | count with
+// tag = 2 (pass + 1) for a tile aggregate and 2 (pass + 1) + 1 for an
+// inclusive prefix; words of earlier passes read as "not ready", so one
+// buffer (zeroed once per sort) serves every pass.
+template <class K>
+__global__ void __launch_bounds__(kSortThreads)
+    k_onesweep(const K *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
+               K *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n,
+               int shift, int pass, const uint32_t *__restrict__ goffsets,
+               unsigned long long *__restrict__ lookback, unsigned *__restrict__ tile_counter,
+               unsigned *__restrict__ err)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PassSmem<K> &sm = *reinterpret_cast<PassSmem<K> *>(smem_raw);
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int warp = tid >> 5;
+
+  if (tid == 0)
+    sm.tile = atomicAdd(tile_counter, 1u);
+  for (int i = tid; i < kSortWarps * (kBins + 1); i += kSortThreads)
+    (&sm.u.whist[0][0])[i] = 0;
+  __syncthreads();
+  const unsigned tile = sm.tile;
+  const int64_t tile_base = (int64_t)tile * kTile;
+
+  // 1. load
+  K key[kItems];
+  uint32_t val[kItems];
+  const int64_t warp_base = tile_base + (int64_t)warp * 32 * kItems + lane;
+#pragma unroll
+  for (int j = 0; j < kItems; ++j)
+  {
+    int64_t idx = warp_base + j * 32;
+    if (idx < n)
+    {
+      key[j] = keys_in[idx];
+      val[j] = vals_in ? vals_in[idx] : (uint32_t)idx;
+    }
+    else
+    {
+      key[j] = 0;
+      val[j] = 0;
+    }
+  }
+
+  // 2. warp-level stable ranking
+  uint32_t rank[kItems];
+  unsigned dig[kItems];
+  const unsigned lt = lanemask_lt();
+#pragma unroll
+  for (int j = 0; j < kItems; ++j)
+  {
+    int64_t idx = warp_base + j * 32;
+    unsigned d = idx < n ? digit_of(key[j], shift) : (unsigned)kBins;
+    dig[j] = d;
+    unsigned peers = __match_any_sync(0xffffffffu, d);
+    int leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader)
+    {
+      base = sm.u.whist[warp][d];
+      sm.u.whist[warp][d] = base + __popc(peers);
+    }
+    base = __shfl_sync(0xffffffffu, base, leader);
+    rank[j] = base + __popc(peers & lt);
+    __syncwarp();
+  }
+  __syncthreads();
+
+  // 3. per-digit warp offsets and tile totals; exclusive scan over digits
+  uint32_t total = 0;
+  {
+    int d = tid;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w)
+    {
+      uint32_t c = sm.u.whist[w][d];
+      sm.u.whist[w][d] = total;
+      total += c;
+    }
+    if (tid == 0)
+    {
+      uint32_t s = 0;
+      for (int w = 0; w < kSortWarps; ++w)
+      {
+        uint32_t c = sm.u.whist[w][kBins];
+        sm.u.whist[w][kBins] = s;
+        s += c;
+      }
+    }
+    uint32_t x = total;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o)
+        x += y;
+    }
+    if (lane == 31)
+      sm.warp_tot[warp] = x;
+    __syncthreads();
+    uint32_t pre = 0;
+    for (int w = 0; w < warp; ++w)
+      pre += sm.warp_tot[w];
+    sm.digit_start[d] = pre + x - total;
+    if (tid == kSortThreads - 1)
+      sm.digit_start[kBins] = pre + x;
+  }
+  __syncthreads();
+
+  uint32_t pos[kItems];
+#pragma unroll
+  for (int j = 0; j < kItems; ++j)
+    pos[j] = sm.digit_start[dig[j]] + sm.u.whist[warp][dig[j]] + rank[j];
+
+  // 4. decoupled look-back, one digit per thread
+  {
+    const int d = tid;
+    const unsigned long long tag_agg = 2ull * (pass + 1);
+    const unsigned long long tag_inc = tag_agg + 1;
+    unsigned long long *row = lookback + (size_t)tile * kBins;
+    uint32_t excl = 0;
+    if (tile == 0)
+    {
+      st_relaxed_u64(&row[d], (tag_inc << 32) | total);
+    }
+    else
+    {
+      st_relaxed_u64(&row[d], (tag_agg << 32) | total);
+      int64_t pred = (int64_t)tile - 1;
+      int spins = 0;
+      while (pred >= 0)
+      {
+        unsigned long long v = ld_relaxed_u64(lookback + (size_t)pred * kBins + d);
+        unsigned long long tag = v >> 32;
+        if (tag < tag_agg)
+        {
+          if (++spins > kSpinLimit)
+          {
+            raise_error(err, ABX_DEVERR_TIMEOUT);
+            break;
+          }
+          continue;
+        }
+        excl += (uint32_t)v;
+        if (tag == tag_inc)
+          break;
+        --pred;
+      }
+      st_relaxed_u64(&row[d], (tag_inc << 32) | (unsigned long long)(excl + total));
+    }
+    sm.gbase[d] = goffsets[d] + excl;
+  }
+  __syncthreads();
+
+  // 5. local scatter in digit order, then coalesced global write
+#pragma unroll
+  for (int j = 0; j < kItems; ++j)
+  {
+    sm.u.exch.keys[pos[j]] = key[j];
+    sm.u.exch.vals[pos[j]] = val[j];
+  }
+  __syncthreads();
+  const uint32_t valid = sm.digit_start[kBins];
+  for (uint32_t i = tid; i < valid; i += kSortThreads)
+  {
+    K k = sm.u.exch.keys[i];
+    unsigned d = digit_of(k, shift);
+    uint32_t g = sm.gbase[d] + (i - sm.digit_start[d]);
+    if (g < n)
+    {
+      keys_out[g] = k;
+      vals_out[g] = sm.u.exch.vals[i];
+    }
+    else
+      raise_error(err, ABX_DEVERR_INTERNAL);
+  }
+}
+
+template <class K>
+abx_status radix_sort_impl(cudaStream_t s, K *d_keys, uint32_t *d_vals,
+                           const uint32_t *d_vals_in, int64_t n, int num_passes,
+                           const uint32_t *d_hist)
+{
+  if (n <= 0)
+    return ABX_SUCCESS;
+  if (n > (int64_t)INT32_MAX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "radix sort: more than 2^31-1 keys");
+  if (num_passes < 1 || num_passes > (int)(sizeof(K) * 8 / 8))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "radix sort: bad number of passes");
+  DeviceState &ds = device_state();
+  const int64_t num_tiles = (n + kTile - 1) / kTile;
+
+  // scratch: [hist passes*256][offsets passes*256][counters 8] lookback
+  const size_t lookback_words = (size_t)num_tiles * kBins;
+  const size_t head_u32 = 2 * kMaxPasses * kBins + kMaxPasses;
+  const size_t head_bytes = (head_u32 * 4 + 255) / 256 * 256;
+  Scratch<unsigned char> work;
+  ABX_CUDA_TRY(work.alloc(head_bytes + lookback_words * 8, s));
+  uint32_t *hist = reinterpret_cast<uint32_t *>(work.ptr);
+  uint32_t *offsets = hist + kMaxPasses * kBins;
+  unsigned *counters = offsets + kMaxPasses * kBins;
+  unsigned long long *lookback = reinterpret_cast<unsigned long long *>(work.ptr + head_bytes);
+  ABX_CUDA_TRY(cudaMemsetAsync(work.ptr, 0, head_bytes + lookback_words * 8, s));
+
+  Scratch<K> keys_alt;
+  Scratch<uint32_t> vals_alt;
+  ABX_CUDA_TRY(keys_alt.alloc(n, s));
+  ABX_CUDA_TRY(vals_alt.alloc(n, s));
+
+  StageScope scope(s, sizeof(K) == 8 ? "sort64" : "sort32", num_passes + (d_hist ? 1 : 2));
+  const uint32_t *hsrc = d_hist;
+  if (!hsrc)
+  {
+    int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ds.num_sms * 8);
+    k_histogram<K><<<blocks, 256, 0, s>>>(d_keys, n, num_passes, hist);
+    hsrc = hist;
+  }
+  k_hist_scan<<<num_passes, kBins, 0, s>>>(hsrc, offsets);
+
+  const size_t smem = sizeof(PassSmem<K>);
+  static bool attr_set = false;
+  if (!attr_set)
+  {
+    ABX_CUDA_TRY(cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+    attr_set = true;
+  }
+
+  const K *kin = d_keys;
+  const uint32_t *vin = d_vals_in;
+  K *kout = keys_alt.ptr;
+  uint32_t *vout = vals_alt.ptr;
+  for (int p = 0; p < num_passes; ++p)
+  {
+    k_onesweep<K><<<(unsigned)num_tiles, kSortThreads, smem, s>>>(
+        kin, vin, kout, vout, n, 8 * p, p, offsets + p * kBins, lookback, counters + p,
+        ds.d_error);
+    ABX_CUDA_TRY(cudaGetLastError());
+    const K *nk = kout;
+    const uint32_t *nv = vout;
+    kout = (kout == keys_alt.ptr) ? d_keys : keys_alt.ptr;
+    vout = (vout == vals_alt.ptr) ? d_vals : vals_alt.ptr;
+    kin = nk;
+    vin = nv;
+  }
+  if (kin != d_keys)
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_keys, kin, n * sizeof(K), cudaMemcpyDeviceToDevice, s));
+  if (vin != d_vals)
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_vals, vin, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  return ABX_SUCCESS;
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan: reduce per chunk, scan the chunk sums, apply.
+// ---------------------------------------------------------------------------
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanChunk = kScanThreads * kScanItems;
+
+__device__ __forceinline__ long long block_sum_ll(long long v, long long *sh)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  long long t = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w)
+      t += sh[w];
+  return t;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(const int32_t *__restrict__ in,
+                                                              int64_t n,
+                                                              long long *__restrict__ sums)
+{
+  __shared__ long long sh[kScanThreads / 32];
+  int64_t base = (int64_t)blockIdx.x * kScanChunk;
+  long long v = 0;
+  for (int j = 0; j < kScanItems; ++j)
+  {
+    int64_t i = base + j * kScanThreads + threadIdx.x;
+    if (i < n)
+      v += in[i];
+  }
+  long long t = block_sum_ll(v, sh);
+  if (threadIdx.x == 0)
+    sums[blockIdx.x] = t;
+}
+
+// Single CTA: exclusive scan of the chunk sums in place (nblocks entries).
+__global__ void __launch_bounds__(1024) k_scan_sums(long long *__restrict__ sums, int64_t nb)
+{
+  __shared__ long long warp_tot[32];
+  __shared__ long long carry;
+  if (threadIdx.x == 0)
+    carry = 0;
+  __syncthreads();
+  for (int64_t base = 0; base < nb; base += blockDim.x)
+  {
+    int64_t i = base + threadIdx.x;
+    long long v = i < nb ? sums[i] : 0;
+    long long x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      long long y = __shfl_up_sync(0xffffffffu, x, o);
+      if ((threadIdx.x & 31) >= o)
+        x += y;
+    }
+    if ((threadIdx.x & 31) == 31)
+      warp_tot[threadIdx.x >> 5] = x;
+    __syncthreads();
+    long long pre = carry;
+    for (int w = 0; w < (int)(threadIdx.x >> 5); ++w)
+      pre += warp_tot[w];
+    if (i < nb)
+      sums[i] = pre + x - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1)
+      carry = pre + x;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int32_t *__restrict__ in,
+                                                             int64_t n,
+                                                             const long long *__restrict__ sums,
+                                                             int32_t *__restrict__ out,
+                                                             unsigned *__restrict__ err)
+{
+  __shared__ long long warp_tot[kScanThreads / 32];
+  int64_t base = (int64_t)blockIdx.x * kScanChunk;
+  // each thread owns kScanItems consecutive elements
+  int64_t first = base + (int64_t)threadIdx.x * kScanItems;
+  int32_t v[kScanItems];
+  long long local = 0;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j)
+  {
+    int64_t i = first + j;
+    v[j] = i < n ? in[i] : 0;
+    local += v[j];
+  }
+  long long x = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1)
+  {
+    long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if ((threadIdx.x & 31) >= o)
+      x += y;
+  }
+  if ((threadIdx.x & 31) == 31)
+    warp_tot[threadIdx.x >> 5] = x;
+  __syncthreads();
+  long long pre = sums[blockIdx.x];
+  for (int w = 0; w < (int)(threadIdx.x >> 5); ++w)
+    pre += warp_tot[w];
+  long long run = pre + x - local;
+#pragma unroll
+  for (int j = 0; j < kScanItems; ++j)
+  {
+    int64_t i = first + j;
+    if (i <= n)
+    {
+      if (run > INT32_MAX)
+        raise_error(err, ABX_DEVERR_BAD_INPUT);
+      if (i < n || j == 0 || first + j - 1 < n)
+        out[i] = (int32_t)run;
+    }
+    run += v[j];
+  }
+}
+
+} // namespace
+
+abx_status radix_sort_u64(cudaStream_t s, uint64_t *d_keys, uint32_t *d_vals,
+                          const uint32_t *d_vals_in, int64_t n, int num_passes,
+                          const uint32_t *d_hist)
+{
+  return radix_sort_impl<uint64_t>(s, d_keys, d_vals, d_vals_in, n, num_passes, d_hist);
+}
+
+abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
+                          const uint32_t *d_vals_in, int64_t n, int num_passes,
+                          const uint32_t *d_hist)
+{
+  return radix_sort_impl<uint32_t>(s, d_keys, d_vals, d_vals_in, n, num_passes, d_hist);
+}
+
+abx_status exclusive_scan_i32(cudaStream_t s, const int32_t *d_in, int64_t n, int32_t *d_out)
+{
+  DeviceState &ds = device_state();
+  if (n < 0)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "exclusive_scan: negative size");
+  int64_t nb = (n + kScanChunk) / kScanChunk; // covers index n as well
+  Scratch<long long> sums;
+  ABX_CUDA_TRY(sums.alloc(nb, s));
+  StageScope scope(s, "scan", 3);
+  k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(d_in, n, sums.ptr);
+  k_scan_sums<<<1, 1024, 0, s>>>(sums.ptr, nb);
+  k_scan_apply<<<(unsigned)nb, kScanThreads, 0, s>>>(d_in, n, sums.ptr, d_out, ds.d_error);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
+
+} // namespace abx

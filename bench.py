@@ -1,0 +1,470 @@
+#!/usr/bin/env python
+"""Benchmark of the BVH hot path: build + nearest(k=16) on 1e7 uniform points.
+
+One step = build a BoundingVolumeHierarchy over N = 10^7 float32 points
+uniform in [0,1)^3 and answer 10^7 nearest(point, k=16) queries drawn from
+the same distribution (CRS output, predicate sorting on, the reference's
+default policy).  `value` is whole-job queries/s of that step with inputs
+resident in HBM; `e2e` is the same step through the public API from pinned
+host buffers (host->device copy of points and queries, device->host copy of
+the CRS indices and offsets inside the timed region).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the reference algorithm on the host cores: the CPU
+restatement of ArborX's construction and nearest traversal (oracle/, the
+reference itself needs Kokkos, absent on both machines), all host threads.
+Multi-GPU (torchrun): every rank runs an independent replica of the
+workload (weak scaling, no collective on the data path).
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "kNN queries/s & BVH build Mpts/s on 1 GB300, batched vs plain, bit-exact"
+N_POINTS = 10_000_000
+N_QUERIES = 10_000_000
+K = 16
+
+# Algorithmic traffic per query of the reference nearest traversal
+# (12 B query + 32 B per internal node visited + 20 B per leaf tested + 4 B per
+# result + 4 B offset), with the visit counts of the reference traversal on
+# this workload measured by the instrumented CPU restatement
+# (oracle/visit_counts.py, 2e4 sampled queries on the 1e7-point tree).
+VISITS_PATH = os.path.join(ROOT, "profiles", "visit_counts.json")
+
+# Algorithmic traffic of the build per point: bounds 12, Morton 12 + 8,
+# 8 radix passes x (12 + 12) + 8 histogram bytes, hierarchy 72.
+BUILD_BYTES_PER_POINT = 304
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=N_POINTS)
+    ap.add_argument("--nq", type=int, default=N_QUERIES)
+    ap.add_argument("--k", type=int, default=K)
+    ap.add_argument("--cpu-sample", type=int, default=1_000_000,
+                    help="queries timed per CPU step (scaled to --nq)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_inputs(n, nq, rank):
+    rng_p = np.random.default_rng(3 + 1000 * rank)
+    rng_q = np.random.default_rng(12 + 1000 * rank)
+    return rng_p.random((n, 3), dtype=np.float32), rng_q.random((nq, 3), dtype=np.float32)
+
+
+def load_visits():
+    try:
+        with open(VISITS_PATH) as f:
+            return json.load(f)
+    except OSError:
+        return None
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+CLOCK_FIELDS = (
+    "index,pci.bus_id,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+    "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+)
+
+
+class ClockSampler:
+    def __init__(self):
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + CLOCK_FIELDS, "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL,
+            )
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self, bus_id=None):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) < 10:
+                    continue
+                rows.append(parts)
+        os.unlink(self.path)
+        if bus_id:
+            mine = [r for r in rows if r[1].lower().endswith(bus_id.lower()[-12:])]
+            rows = mine or rows
+        if not rows:
+            return None
+        try:
+            sm = [float(r[2]) for r in rows]
+            smax = max(float(r[3]) for r in rows)
+        except ValueError:
+            return None
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for name, v in zip(names, r[6:10]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        loaded = sorted(sm)
+        return {
+            "sm_mhz": float(np.median(loaded)),
+            "sm_max_mhz": smax,
+            "reasons": sorted(reasons),
+            "samples": len(rows),
+        }
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference algorithm restated (oracle/), all host threads
+# ---------------------------------------------------------------------------
+
+
+def cpu_step(points, queries, k, sample):
+    from oracle import oracle as orc
+
+    t0 = time.perf_counter()
+    tree = orc.OracleTree(points)
+    t1 = time.perf_counter()
+    m = min(sample, len(queries))
+    tree.nearest(queries[:m], k, mode=orc.MODE_ARBORX)
+    t2 = time.perf_counter()
+    scale = len(queries) / m
+    return (t1 - t0), (t2 - t1) * scale
+
+
+def cpu_baseline(points, queries, k, sample, steps=1):
+    from oracle import oracle as orc
+
+    threads = orc.num_threads()
+    best = None
+    for _ in range(steps):
+        tb, tq = cpu_step(points, queries, k, sample)
+        if best is None or tb + tq < best[0] + best[1]:
+            best = (tb, tq)
+    tb, tq = best
+    return {
+        "value": len(queries) / (tb + tq),
+        "unit": "queries/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": "build over all %d points + nearest(k=%d) on %d of %d queries, query time scaled"
+        % (len(points), k, min(sample, len(queries)), len(queries)),
+        "build_mpts_per_s": len(points) / tb / 1e6,
+    }
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+
+    orc.build_oracle()
+    points, queries = make_inputs(args.n, args.nq, 0)
+    for _ in range(args.warmup):
+        cpu_step(points, queries, args.k, args.cpu_sample)
+    times = []
+    builds = []
+    for _ in range(args.steps):
+        tb, tq = cpu_step(points, queries, args.k, args.cpu_sample)
+        times.append(tb + tq)
+        builds.append(tb)
+    t = float(np.median(times))
+    value = args.nq / t
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": "queries/s",
+        "n_gpus": args.gpus,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": t * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic: seeded uniform [0,1)^3 points and queries",
+        "config": config_of(args),
+        "build": {"value": args.n / float(np.median(builds)) / 1e6, "unit": "Mpts/s"},
+        "cpu_baseline": {
+            "value": value,
+            "unit": "queries/s",
+            "cores": orc.num_threads(),
+            "kind": "port",
+            "sample": "per step: build over all %d points + ArborX nearest traversal (k=%d) on %d of %d "
+            "queries, query time scaled; CPU restatement of the reference (Kokkos absent)"
+            % (args.n, args.k, min(args.cpu_sample, args.nq), args.nq),
+        },
+        "e2e": {"value": value, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args):
+    return {
+        "workload": "knn_uniform_1e7_k16: BVH build over %d uniform points + %d nearest(k=%d) queries per step"
+        % (args.n, args.nq, args.k),
+        "n_points": args.n,
+        "n_queries": args.nq,
+        "k": args.k,
+        "policy": "sort_predicates=true (reference default)",
+        "l2": "inputs larger than L2: points %.0f MB, queries %.0f MB, tree %.0f MB per step vs 126 MB L2"
+        % (args.n * 12 / 1e6, args.nq * 12 / 1e6, args.n * 104 / 1e6),
+        "parallelism": "replicas (one independent problem per GPU)",
+    }
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    import arborx_gb300 as ax
+    from arborx_gb300 import _lib
+    from arborx_gb300 import build as libbuild
+
+    libbuild.build()
+    L = _lib.load()
+
+    points_np, queries_np = make_inputs(args.n, args.nq, rank)
+    points_h = torch.from_numpy(points_np).pin_memory()
+    queries_h = torch.from_numpy(queries_np).pin_memory()
+    points = points_h.cuda()
+    queries = queries_h.cuda()
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def step():
+        bvh = ax.BoundingVolumeHierarchy(points)
+        ind, off = ax.query(bvh, ax.nearest(queries, args.k))
+        return bvh, ind, off
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    for _ in range(args.warmup):
+        keep = step()
+    del keep
+    barrier()
+
+    # --- device-resident steps, stage profiling on -----------------------
+    def profiled(fn, steps):
+        L.abx_profiling_reset()
+        L.abx_profiling_enable(1)
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        keep = None
+        for _ in range(steps):
+            keep = fn()
+        e1.record(stream)
+        barrier()
+        L.abx_profiling_enable(0)
+        del keep
+        return e0.elapsed_time(e1) / steps
+
+    clocks = ClockSampler()
+    clocks.start()
+    ms_step = max_over_ranks(profiled(step, args.steps))
+    clk = clocks.stop(getattr(torch.cuda.get_device_properties(local), "pci_bus_id", None))
+
+    import ctypes
+
+    def stage(name):
+        ms = ctypes.c_double(0)
+        cnt = ctypes.c_int64(0)
+        _lib.check(L.abx_profiling_stage(name.encode(), ctypes.byref(ms), ctypes.byref(cnt)))
+        return ms.value / args.steps, cnt.value
+
+    stages = {s: stage(s) for s in ("bounds", "morton64", "sort64", "hierarchy", "morton32", "sort32", "nearest")}
+    all_ms, launches = stage("*")
+    L.abx_profiling_reset()
+
+    build_ms = sum(stages[s][0] for s in ("bounds", "morton64", "sort64", "hierarchy"))
+    nearest_ms = stages["nearest"][0]
+
+    # --- end to end through the public API from pinned host memory ------
+    out_idx_h = torch.empty(args.nq * min(args.k, args.n), dtype=torch.int32).pin_memory()
+    out_off_h = torch.empty(args.nq + 1, dtype=torch.int32).pin_memory()
+
+    def e2e_step():
+        p = points_h.to("cuda", non_blocking=True)
+        q = queries_h.to("cuda", non_blocking=True)
+        bvh = ax.BoundingVolumeHierarchy(p)
+        ind, off = ax.query(bvh, ax.nearest(q, args.k))
+        out_idx_h.copy_(ind, non_blocking=True)
+        out_off_h.copy_(off, non_blocking=True)
+        return bvh, ind, off, p, q
+
+    for _ in range(2):
+        keep = e2e_step()
+    del keep
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        keep = e2e_step()
+    e1.record(stream)
+    barrier()
+    del keep
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps)
+    h2d = args.n * 12 + args.nq * 12
+    d2h = out_idx_h.numel() * 4 + out_off_h.numel() * 4
+
+    # --- roofline of the dominant kernel ----------------------------------
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    visits = load_visits()
+    if visits and visits.get("n") == args.n and visits.get("k") == args.k:
+        per_query = 12 + 32 * visits["internal"] + 20 * visits["leaves"] + 4 * args.k + 4
+        bytes_src = "reference traversal visit counts (profiles/visit_counts.json)"
+    else:
+        per_query = 12 + 64 * 2 * 20 + 4 * args.k + 4
+        bytes_src = "estimate (visit counts not measured for this size)"
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "ncu_traffic.json")) as f:
+            tr = json.load(f).get("k_nearest")
+            if tr and tr.get("n") == args.n and tr.get("nq") == args.nq:
+                traffic = tr["bytes_per_launch"]
+    except OSError:
+        pass
+    achieved = per_query * args.nq / (nearest_ms * 1e-3) / 1e9
+    roofline = {
+        "kernel": "k_nearest<16>",
+        "bound": "hbm",
+        "achieved": achieved,
+        "peak": hbm_peak,
+        "unit": "GB/s",
+        "frac": achieved / hbm_peak,
+        "traffic": traffic,
+        "algorithmic_bytes_per_query": per_query,
+        "bytes_source": bytes_src,
+        "peak_source": peak_src,
+        "kernel_ms": nearest_ms,
+    }
+    build_achieved = BUILD_BYTES_PER_POINT * args.n / (build_ms * 1e-3) / 1e9
+    value = args.nq * world / (ms_step * 1e-3)
+
+    line = None
+    if rank == 0:
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": "queries/s",
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": ms_step,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f32",
+            "data": "synthetic: seeded uniform [0,1)^3 points and queries (numpy PCG64)",
+            "config": config_of(args),
+            "queries_k_per_s": value * args.k,
+            "build": {
+                "value": args.n * world / (build_ms * 1e-3) / 1e6,
+                "unit": "Mpts/s",
+                "ms": build_ms,
+                "hbm_frac": build_achieved / hbm_peak,
+                "algorithmic_bytes_per_point": BUILD_BYTES_PER_POINT,
+            },
+            "stages_ms": {k: v[0] for k, v in stages.items()},
+            "e2e": {
+                "value": args.nq * world / (e2e_ms * 1e-3),
+                "unit": "queries/s",
+                "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h,
+            },
+            "roofline": roofline,
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            cpu = cpu_baseline(points_np, queries_np, args.k, args.cpu_sample)
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,236 @@
+/*
+ * arborx_gb300.h -- C ABI of the GB300-native bounding volume hierarchy.
+ *
+ * A drop-in for the ArborX BoundingVolumeHierarchy hot path (construction,
+ * intersects / nearest queries, CRS output), implemented with hand-written
+ * sm_103a CUDA kernels.  Every pointer argument named d_* is DEVICE memory;
+ * h_* is host memory.  Streams are cudaStream_t passed as void* (NULL = the
+ * legacy default stream).  Every call is stream-ordered; the documented
+ * synchronisation points are the same as the reference's (root bounds after a
+ * build, the result count of a two-pass spatial query).
+ *
+ * Each declaration cites the reference interface it replaces (paths relative
+ * to the ArborX source tree, version 2.1.99).
+ */
+#ifndef ARBORX_GB300_H
+#define ARBORX_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define ABX_API __attribute__((visibility("default")))
+#else
+#define ABX_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference reports errors by throwing
+ * ArborX::SearchException from ARBORX_ASSERT (src/misc/ArborX_Exception.hpp:
+ * 19-37); no C++ exception crosses this ABI, each call returns one of these. */
+typedef enum abx_status
+{
+  ABX_SUCCESS = 0,
+  ABX_ERROR_INVALID_ARGUMENT = 1, /* ARBORX_ASSERT on a precondition          */
+  ABX_ERROR_CUDA = 2,             /* a CUDA runtime call failed               */
+  ABX_ERROR_OUT_OF_MEMORY = 3,    /* device allocation failed                 */
+  ABX_ERROR_BUFFER_OVERFLOW = 4,  /* hard preallocation too small
+                                     (ArborX_CrsGraphWrapperImpl.hpp:268)     */
+  ABX_ERROR_DEVICE = 5,           /* a kernel raised the device error word    */
+  ABX_ERROR_NOT_SUPPORTED = 6,
+  ABX_ERROR_TIMEOUT = 7           /* a bounded device-side wait gave up       */
+} abx_status;
+
+/* Bits of the device error word (abx_device_errors). */
+#define ABX_DEVERR_STACK_OVERFLOW 0x1u
+#define ABX_DEVERR_TIMEOUT 0x2u
+#define ABX_DEVERR_BAD_INPUT 0x4u
+#define ABX_DEVERR_INTERNAL 0x8u
+
+typedef struct abx_bvh abx_bvh; /* opaque tree                                */
+typedef struct abx_crs abx_crs; /* opaque CRS result (offsets + indices)      */
+
+/* Geometry of values and predicates, float32, array-of-structures:
+ *   POINT  x y z                 (12 bytes)   ArborX::Point<3>
+ *   BOX    minx miny minz maxx maxy maxz (24) ArborX::Box<3>
+ *   SPHERE cx cy cz r            (16 bytes)   ArborX::Sphere<3>
+ * (src/geometry/ArborX_Point.hpp:24-38, ArborX_Box.hpp:32-67,
+ *  ArborX_Sphere.hpp:25-47). */
+typedef enum abx_geometry
+{
+  ABX_POINT = 0,
+  ABX_BOX = 1,
+  ABX_SPHERE = 2
+} abx_geometry;
+
+/* TraversalPolicy (src/spatial/detail/ArborX_TraversalPolicy.hpp:19-47):
+ * buffer_size 0 = two-pass count/fill; > 0 = single pass into a per-query
+ * buffer, second pass on overflow; < 0 = single pass, overflow is an error.
+ * sort_predicates: reorder queries along Morton32 of their centroids
+ * (ArborX_LinearBVH.hpp:287-306), default 1. */
+typedef struct abx_traversal_policy
+{
+  int32_t buffer_size;
+  int32_t sort_predicates;
+} abx_traversal_policy;
+
+/* ---------------------------------------------------------------------- */
+/* Library                                                                  */
+/* ---------------------------------------------------------------------- */
+
+/* Human-readable name of a status. */
+ABX_API const char *abx_status_string(abx_status status);
+
+/* Detailed message of the last failing call on this host thread. */
+ABX_API const char *abx_last_error(void);
+
+/* Library version "major.minor.patch". */
+ABX_API const char *abx_version(void);
+
+/* Read and clear the device error word of the current device
+ * (ABX_DEVERR_* bits); synchronises `stream`.  Replaces the reference's
+ * device-side KOKKOS_ASSERT/abort (ArborX_HappyTreeFriends.hpp:28-62),
+ * which would kill the context. */
+ABX_API abx_status abx_device_errors(void *stream, uint32_t *h_bits);
+
+/* Stage timing, the counterpart of the reference's Kokkos Tools regions
+ * (ArborX_LinearBVH.hpp:201-255, ArborX_CrsGraphWrapperImpl.hpp:394-431).
+ * While enabled, every kernel stage of every call records a pair of CUDA
+ * events on the stream it runs on.  abx_profiling_stage waits for the
+ * recorded events and returns the summed device time and the number of
+ * kernel launches of one stage ("bounds", "morton64", "sort64",
+ * "hierarchy", "morton32", "sort32", "spatial", "scan", "compact",
+ * "nearest"); "*" sums all stages.  abx_profiling_reset drops the records. */
+ABX_API abx_status abx_profiling_enable(int32_t enable);
+ABX_API abx_status abx_profiling_stage(const char *stage, double *h_total_ms,
+                                       int64_t *h_launches);
+ABX_API abx_status abx_profiling_reset(void);
+
+/* ---------------------------------------------------------------------- */
+/* Tree                                                                     */
+/* ---------------------------------------------------------------------- */
+
+/* BoundingVolumeHierarchy(space, values[, indexable_getter, Morton64{}])
+ * (src/spatial/ArborX_LinearBVH.hpp:68-73,167-256).  `d_values` holds n
+ * points (ABX_POINT) or boxes (ABX_BOX) in device memory; the value stored in
+ * every leaf is its index in d_values (the benchmark form
+ * BVH<MemorySpace, int, IndexableGetter>, benchmarks/bvh_driver/
+ * benchmark_registration.hpp:151-161).  The geometry is copied; d_values may
+ * be freed after the call returns.  Asynchronous on `stream`. */
+ABX_API abx_status abx_bvh_create(void *stream, abx_geometry kind,
+                          const float *d_values, int64_t n, abx_bvh **out);
+
+/* Destroy a tree (frees stream-ordered on the stream it was built on). */
+ABX_API abx_status abx_bvh_destroy(abx_bvh *bvh);
+
+/* size() / empty() (ArborX_LinearBVH.hpp:75-79). */
+ABX_API int64_t abx_bvh_size(const abx_bvh *bvh);
+
+/* bounds() (ArborX_LinearBVH.hpp:81-82): the root bounding box, the empty
+ * box [FLT_MAX, -FLT_MAX] for an empty tree.  Waits for the build. */
+ABX_API abx_status abx_bvh_bounds(const abx_bvh *bvh, float h_box[6]);
+
+/* Geometry kind of the leaves. */
+ABX_API abx_geometry abx_bvh_geometry(const abx_bvh *bvh);
+
+/* Copy the node arrays in the reference layout to device buffers
+ * (src/spatial/detail/ArborX_Node.hpp:24-51): d_leaves receives n
+ * {int32 rope, int32 value}; d_internal receives n-1 {int32 left_child,
+ * int32 rope, float box[6]} (32 bytes each).  Node numbering follows
+ * ArborX_HappyTreeFriends.hpp:23-86.  Either pointer may be NULL. */
+ABX_API abx_status abx_bvh_export_nodes(const abx_bvh *bvh, void *stream,
+                                int32_t *d_leaves, void *d_internal);
+
+/* ---------------------------------------------------------------------- */
+/* Queries with CRS output                                                  */
+/* ---------------------------------------------------------------------- */
+
+/* query(space, intersects(geometry)..., indices, offsets, policy)
+ * (ArborX_LinearBVH.hpp:90-110; ArborX_CrsGraphWrapper.hpp:22-34;
+ * ArborX_CrsGraphWrapperImpl.hpp:378-432).  `kind` is the predicate geometry
+ * (ABX_SPHERE or ABX_BOX), d_predicates holds nq of them.  The result owns
+ * its device arrays (the reference reallocates out/offset in the callee,
+ * ArborX_CrsGraphWrapperImpl.hpp:286,376-377).  The call synchronises
+ * `stream` once to size the output, like the reference's lastElement
+ * (ArborX_CrsGraphWrapperImpl.hpp:248). */
+ABX_API abx_status abx_bvh_query_intersects(const abx_bvh *bvh, void *stream,
+                                    abx_geometry kind,
+                                    const float *d_predicates, int64_t nq,
+                                    abx_traversal_policy policy,
+                                    abx_crs **out);
+
+/* query(space, nearest(point, k)..., indices, offsets[, policy])
+ * (ArborX_CrsGraphWrapperImpl.hpp:353-374; TreeTraversal<Nearest>,
+ * ArborX_TreeTraversal.hpp:122-336).  d_queries: nq points.  d_k: one k per
+ * query (device int32) or NULL to use `k` for all.  Each query returns
+ * min(k, size()) values ordered by ascending (distance, index): the k
+ * smallest float32 distances, ties at equal distance broken by the smaller
+ * value index.  With with_distances != 0 the distances are kept
+ * (abx_crs_distances).  Asynchronous unless d_k is given (then one
+ * synchronisation to size the output). */
+ABX_API abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream,
+                                 const float *d_queries, int64_t nq,
+                                 const int32_t *d_k, int32_t k,
+                                 abx_traversal_policy policy,
+                                 int32_t with_distances, abx_crs **out);
+
+/* Accessors of a CRS result: device offsets (nq + 1), device indices
+ * (num_results), device distances (nearest only, else NULL). */
+ABX_API int64_t abx_crs_num_queries(const abx_crs *crs);
+ABX_API int64_t abx_crs_num_results(const abx_crs *crs);
+ABX_API const int32_t *abx_crs_offsets(const abx_crs *crs);
+ABX_API const int32_t *abx_crs_indices(const abx_crs *crs);
+ABX_API const float *abx_crs_distances(const abx_crs *crs);
+ABX_API abx_status abx_crs_destroy(abx_crs *crs);
+
+/* ---------------------------------------------------------------------- */
+/* Building blocks (the reference's Details functions, exposed for parity  */
+/* tests and for callers that assemble their own pipelines)               */
+/* ---------------------------------------------------------------------- */
+
+/* calculateBoundingBoxOfTheScene (spatial/detail/
+ * ArborX_TreeConstruction.hpp:26-39): d_box_out receives 6 floats. */
+ABX_API abx_status abx_scene_bounds(void *stream, abx_geometry kind,
+                            const float *d_values, int64_t n,
+                            float *d_box_out);
+
+/* projectOntoSpaceFillingCurve with Morton64 (spatial/detail/
+ * ArborX_SpaceFillingCurves.hpp:45-57,64-84) against the scene box
+ * d_scene (6 floats). */
+ABX_API abx_status abx_morton64(void *stream, abx_geometry kind,
+                        const float *d_values, int64_t n,
+                        const float *d_scene, uint64_t *d_codes);
+
+/* Morton32 of predicate centroids (ArborX_SpaceFillingCurves.hpp:30-43). */
+ABX_API abx_status abx_morton32(void *stream, abx_geometry kind,
+                        const float *d_values, int64_t n,
+                        const float *d_scene, uint32_t *d_codes);
+
+/* sortObjects (misc/ArborX_SortUtils.hpp:28-39): sort d_keys in place
+ * (stable: equal keys keep their input order) and write the permutation. */
+ABX_API abx_status abx_sort_u64(void *stream, uint64_t *d_keys, int64_t n,
+                        uint32_t *d_permutation);
+ABX_API abx_status abx_sort_u32(void *stream, uint32_t *d_keys, int64_t n,
+                        uint32_t *d_permutation);
+
+/* generateHierarchy (spatial/detail/ArborX_TreeConstruction.hpp:71-348)
+ * from already sorted Morton codes and the permutation: writes the node
+ * arrays in the layout of abx_bvh_export_nodes.  n >= 2. */
+ABX_API abx_status abx_generate_hierarchy(void *stream, abx_geometry kind,
+                                  const float *d_values, int64_t n,
+                                  const uint32_t *d_permutation,
+                                  const uint64_t *d_sorted_codes,
+                                  int32_t *d_leaves, void *d_internal);
+
+/* exclusive_scan (kokkos_ext/ArborX_KokkosExtStdAlgorithms.hpp:24) of n
+ * int32 into n + 1 outputs (the last is the total).  In-place allowed. */
+ABX_API abx_status abx_exclusive_scan_i32(void *stream, const int32_t *d_in,
+                                  int64_t n, int32_t *d_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ARBORX_GB300_H */
