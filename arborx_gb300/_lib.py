@@ -69,7 +69,11 @@ SIGNATURES = {
     "abx_sort_u32": (_STATUS, [_P, _P, _I64, _P]),
     "abx_generate_hierarchy": (_STATUS, [_P, ctypes.c_int, _P, _I64, _P, _P, _P, _P]),
     "abx_exclusive_scan_i32": (_STATUS, [_P, _P, _I64, _P]),
+    "abx_exclusive_scan_i32_noalloc": (_STATUS, [_P, _P, _I64, _P]),
 }
+
+# Largest input of abx_exclusive_scan_i32_noalloc (ABX_NOALLOC_SCAN_MAX_N).
+NOALLOC_SCAN_MAX_N = 16777216
 
 
 class AbxError(RuntimeError):

@@ -17,6 +17,7 @@
 //   5. scatter the tile into shared memory in digit order, then write it out
 //      so that equal-digit runs land on consecutive global addresses.
 #include <algorithm>
+#include <mutex>
 
 #include "abx_common.cuh"
 #include "abx_internal.h"
@@ -528,4 +529,68 @@ abx_status exclusive_scan_i32(cudaStream_t s, const int32_t *d_in, int64_t n, in
   return ABX_SUCCESS;
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free exclusive scan (abx_exclusive_scan_i32_noalloc)
+// ---------------------------------------------------------------------------
+
+namespace
+{
+
+constexpr int64_t kNoAllocScanMaxN = ABX_NOALLOC_SCAN_MAX_N;
+constexpr int64_t kNoAllocScanChunks = kNoAllocScanMaxN / kScanChunk + 1;
+
+// The scan's chunk sums live in the library's static device memory: no call
+// allocates.  Shared by every call on a device (see the header for the
+// consequences: overlapping calls race).
+static __device__ __align__(256) long long g_noalloc_scan_sums[kNoAllocScanChunks];
+
+std::mutex g_noalloc_mutex;
+long long *g_noalloc_sums_ptr[64] = {};
+
+// Device address of g_noalloc_scan_sums for the current device, looked up
+// once per device.  In host code the array's name is only a host-side
+// stand-in, never a device address.
+abx_status noalloc_scan_scratch(long long **out)
+{
+  int dev = 0;
+  ABX_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64)
+    return fail(ABX_ERROR_NOT_SUPPORTED, "abx_exclusive_scan_i32_noalloc: device id >= 64");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_sums_ptr[dev])
+  {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan_sums);
+    if (e != cudaSuccess)
+      return fail_cuda(e, "cudaGetSymbolAddress(g_noalloc_scan_sums)");
+    g_noalloc_sums_ptr[dev] = static_cast<long long *>(p);
+  }
+  *out = g_noalloc_sums_ptr[dev];
+  return ABX_SUCCESS;
+}
+
+} // namespace
+
 } // namespace abx
+
+extern "C" abx_status abx_exclusive_scan_i32_noalloc(void *stream, const int32_t *d_in,
+                                                      int64_t n, int32_t *d_out)
+{
+  using namespace abx;
+  if (n < 0 || !d_out || (n > 0 && !d_in))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_exclusive_scan_i32_noalloc: bad argument");
+  if (n > kNoAllocScanMaxN)
+    return fail(ABX_ERROR_INVALID_ARGUMENT,
+                "abx_exclusive_scan_i32_noalloc: n = " + std::to_string(n) +
+                    " exceeds the maximum of " + std::to_string(kNoAllocScanMaxN) +
+                    " inputs this allocation-free variant supports");
+  long long *sums = nullptr;
+  ABX_TRY(noalloc_scan_scratch(&sums));
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  const int64_t nb = (n + kScanChunk) / kScanChunk; // <= kNoAllocScanChunks
+  k_scan_reduce<<<(unsigned)nb, kScanThreads, 0, s>>>(d_in, n, sums);
+  k_scan_sums<<<1, 1024, 0, s>>>(sums, nb);
+  k_scan_apply<<<(unsigned)nb, kScanThreads, 0, s>>>(d_in, n, sums, d_out, nullptr);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}

@@ -229,6 +229,36 @@ ABX_API abx_status abx_generate_hierarchy(void *stream, abx_geometry kind,
 ABX_API abx_status abx_exclusive_scan_i32(void *stream, const int32_t *d_in,
                                   int64_t n, int32_t *d_out);
 
+/* Allocation-free exclusive scan.  No counterpart in the reference: ArborX
+ * always allocates its scratch through Kokkos.
+ *
+ * For callers that must not allocate device memory: code that runs under a
+ * device-memory budget owned by another allocator (a framework that has
+ * reserved the GPU's memory for its own pool, where an extra cudaMalloc can
+ * fail or break that pool's accounting), and latency-critical loops that
+ * must not take the allocator's locks or the device-wide synchronisation of
+ * cudaFree.  It computes exactly what abx_exclusive_scan_i32 computes (n
+ * int32 inputs, n + 1 outputs, in place allowed) for
+ * n <= ABX_NOALLOC_SCAN_MAX_N and rejects larger n with
+ * ABX_ERROR_INVALID_ARGUMENT.  It allocates nothing: its scratch (one 64-bit
+ * partial sum per 4096 inputs, 32 KB in all) is a static array in the
+ * library's device memory, which every GPU that loads the library holds
+ * until the process exits.
+ *
+ * The first call on a device, with that device current, looks up the
+ * array's device address (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the one array: calls that
+ * overlap on the GPU (on different streams with no ordering between them)
+ * race and corrupt each other's result, so order them on one stream or with
+ * events.  Each call writes every scratch entry before reading it, so no
+ * entry has to start at zero.  The total must fit in int32: unlike
+ * abx_exclusive_scan_i32, this variant does not report an overflowing total
+ * in the device error word. */
+#define ABX_NOALLOC_SCAN_MAX_N 16777216
+ABX_API abx_status abx_exclusive_scan_i32_noalloc(void *stream,
+                                                  const int32_t *d_in,
+                                                  int64_t n, int32_t *d_out);
+
 #ifdef __cplusplus
 }
 #endif
