@@ -21,9 +21,7 @@ workload (weak scaling, no collective on the data path).
 import argparse
 import json
 import os
-import subprocess
 import sys
-import tempfile
 import time
 
 import numpy as np
@@ -88,70 +86,88 @@ def load_visits():
 # clocks
 # ---------------------------------------------------------------------------
 
-CLOCK_FIELDS = (
-    "index,pci.bus_id,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-    "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-    "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
-)
-
-
 class ClockSampler:
-    def __init__(self):
-        self.proc = None
-        self.path = None
+    """Samples SM clocks and clock-event reasons through NVML (ctypes, read
+    only) every 20 ms on a background thread while the timed region runs."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, pci_bus_id=None):
+        import ctypes
+        import threading
+
+        self._ct = ctypes
+        self.samples = []
+        self.reasons = 0
+        self.max_mhz = None
+        self.ok = False
+        self._stop = threading.Event()
+        self._thread = None
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            found = False
+            if pci_bus_id:
+                found = nv.nvmlDeviceGetHandleByPciBusId_v2(pci_bus_id.encode(), ctypes.byref(h)) == 0
+            if not found:
+                cnt = ctypes.c_uint(0)
+                nv.nvmlDeviceGetCount_v2(ctypes.byref(cnt))
+                if cnt.value != 1:
+                    return
+                found = nv.nvmlDeviceGetHandleByIndex_v2(0, ctypes.byref(h)) == 0
+            if not found:
+                return
+            mx = ctypes.c_uint(0)
+            if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) == 0:
+                self.max_mhz = float(mx.value)
+            self._reason_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or getattr(
+                nv, "nvmlDeviceGetCurrentClocksThrottleReasons"
+            )
+            self.nv, self.h, self.ok = nv, h, True
+            self._thread = threading.Thread(target=self._run, daemon=True)
+        except (OSError, AttributeError):
+            self.ok = False
+
+    def _run(self):
+        ct = self._ct
+        clk = ct.c_uint(0)
+        rs = ct.c_ulonglong(0)
+        while not self._stop.is_set():
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) == 0:
+                self.samples.append(float(clk.value))
+            if self._reason_fn(self.h, ct.byref(rs)) == 0:
+                self.reasons |= rs.value
+            self._stop.wait(0.02)
 
     def start(self):
-        try:
-            fd, self.path = tempfile.mkstemp(suffix=".csv")
-            os.close(fd)
-            self.f = open(self.path, "w")
-            self.proc = subprocess.Popen(
-                ["nvidia-smi", "--query-gpu=" + CLOCK_FIELDS, "--format=csv,noheader,nounits", "-lms", "200"],
-                stdout=self.f, stderr=subprocess.DEVNULL,
-            )
-        except (OSError, FileNotFoundError):
-            self.proc = None
+        if self._thread:
+            self._thread.start()
 
-    def stop(self, bus_id=None):
-        if self.proc is None:
+    def stop(self):
+        if not self._thread:
             return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
-        self.f.close()
-        rows = []
-        with open(self.path) as f:
-            for line in f:
-                parts = [x.strip() for x in line.split(",")]
-                if len(parts) < 10:
-                    continue
-                rows.append(parts)
-        os.unlink(self.path)
-        if bus_id:
-            mine = [r for r in rows if r[1].lower().endswith(bus_id.lower()[-12:])]
-            rows = mine or rows
-        if not rows:
+        self._stop.set()
+        self._thread.join()
+        if not self.samples:
             return None
-        try:
-            sm = [float(r[2]) for r in rows]
-            smax = max(float(r[3]) for r in rows)
-        except ValueError:
-            return None
-        reasons = set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            for name, v in zip(names, r[6:10]):
-                if v.lower().startswith("active"):
-                    reasons.add(name)
-        loaded = sorted(sm)
         return {
-            "sm_mhz": float(np.median(loaded)),
-            "sm_max_mhz": smax,
-            "reasons": sorted(reasons),
-            "samples": len(rows),
+            "sm_mhz": float(np.median(self.samples)),
+            "sm_max_mhz": self.max_mhz,
+            "reasons": sorted(v for k, v in self.REASONS.items() if self.reasons & k),
+            "samples": len(self.samples),
+            "source": "NVML every 20 ms during the timed steps",
         }
+
+
+def pci_bus_id(torch, dev):
+    p = torch.cuda.get_device_properties(dev)
+    try:
+        return "%08X:%02X:%02X.0" % (p.pci_domain_id, p.pci_bus_id, p.pci_device_id)
+    except AttributeError:
+        return None
 
 
 # ---------------------------------------------------------------------------
@@ -323,10 +339,10 @@ def run_gpu(args):
         del keep
         return e0.elapsed_time(e1) / steps
 
-    clocks = ClockSampler()
+    clocks = ClockSampler(pci_bus_id(torch, local))
     clocks.start()
     ms_step = max_over_ranks(profiled(step, args.steps))
-    clk = clocks.stop(getattr(torch.cuda.get_device_properties(local), "pci_bus_id", None))
+    clk = clocks.stop()
 
     import ctypes
 

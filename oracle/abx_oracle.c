@@ -765,8 +765,20 @@ static inline float nearest_dist(const tree_t *t, const float q[3], int node)
  * only when strictly closer than the current k-th distance, the closer child
  * is visited first (ties -> left), and the final order is the heap sort's.
  * `buf` has room for k pairs.  Returns the number of results (min(k, n)). */
+static int64_t nearest_arborx_counted(const tree_t *t, const float q[3], int k,
+                                      pair_t *buf, int64_t *visits);
+
 static int64_t nearest_arborx(const tree_t *t, const float q[3], int k,
                               pair_t *buf)
+{
+  return nearest_arborx_counted(t, q, k, buf, NULL);
+}
+
+/* visits (optional): [0] internal nodes read (root + internal children whose
+ * distance is computed), [1] leaves read (leaf children whose distance is
+ * computed).  These are the node reads of the reference traversal. */
+static int64_t nearest_arborx_counted(const tree_t *t, const float q[3], int k,
+                                      pair_t *buf, int64_t *visits)
 {
   if (k < 1 || t->n == 0)
     return 0;
@@ -787,6 +799,8 @@ static int64_t nearest_arborx(const tree_t *t, const float q[3], int k,
   int left_child = 0, right_child = 0;
   float distance_left = 0.f, distance_right = 0.f, distance_node = 0.f;
   float radius = INFINITY;
+  if (visits)
+    visits[0]++;
   do
   {
     int traverse_left = 0, traverse_right = 0;
@@ -794,6 +808,11 @@ static int64_t nearest_arborx(const tree_t *t, const float q[3], int k,
     {
       left_child = t->internal[node - t->n].left_child;
       right_child = node_rope(t, left_child);
+      if (visits)
+      {
+        visits[left_child < t->n ? 1 : 0]++;
+        visits[right_child < t->n ? 1 : 0]++;
+      }
       distance_left = nearest_dist(t, q, left_child);
       distance_right = nearest_dist(t, q, right_child);
       if (distance_left < radius)
@@ -1103,4 +1122,59 @@ void abxo_exclusive_scan_i32(const int32_t *in, int64_t n, int32_t *out)
     out[i] = (int32_t)s;
     s += v;
   }
+}
+
+/* Node reads of the rope walk: [0] internal nodes tested, [1] leaves tested. */
+static void spatial_visits(const tree_t *t, int kind, const float *pred, int64_t *visits)
+{
+  if (t->n < 2)
+  {
+    visits[1] += t->n;
+    return;
+  }
+  int node = (int)t->n;
+  do
+  {
+    if (node < t->n)
+    {
+      visits[1]++;
+      node = t->leaves[node].rope;
+    }
+    else
+    {
+      visits[0]++;
+      node = spatial_test(t, kind, pred, node) ? t->internal[node - t->n].left_child
+                                               : t->internal[node - t->n].rope;
+    }
+  } while (node != ABXO_ROPE_SENTINEL);
+}
+
+/* Sum of node reads over a batch of queries, for algorithmic byte counts.
+ * mode 0: nearest (queries are points, k), mode 1: spatial (kind, preds). */
+void abxo_visit_counts(int64_t n, int is_box, const float *geom,
+                       const abxo_leaf *leaves, const abxo_internal *internal,
+                       int mode, int kind, const float *preds, int64_t nq,
+                       int32_t k, int64_t *out_internal, int64_t *out_leaves)
+{
+  tree_t t = {n, is_box, geom, leaves, internal};
+  int64_t vi = 0, vl = 0;
+  int stride = mode == 0 ? 3 : (kind == 1 ? 4 : 6);
+#pragma omp parallel reduction(+ : vi, vl)
+  {
+    pair_t *buf = (pair_t *)malloc(sizeof(pair_t) * (k > 0 ? k : 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t q = 0; q < nq; ++q)
+    {
+      int64_t v[2] = {0, 0};
+      if (mode == 0)
+        nearest_arborx_counted(&t, preds + stride * q, k, buf, v);
+      else
+        spatial_visits(&t, kind, preds + stride * q, v);
+      vi += v[0];
+      vl += v[1];
+    }
+    free(buf);
+  }
+  *out_internal = vi;
+  *out_leaves = vl;
 }

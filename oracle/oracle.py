@@ -77,6 +77,7 @@ def lib():
         L.abxo_spatial_brute.restype = I64
         L.abxo_spatial_brute.argtypes = [P, I64, I, I, P, I64, P, P]
         L.abxo_exclusive_scan_i32.argtypes = [P, I64, P]
+        L.abxo_visit_counts.argtypes = [I64, I, P, P, P, I, I, P, I64, I32, P, P]
         L.abxo_num_threads.restype = I
         L.abxo_set_num_threads.argtypes = [I]
         _lib = L
@@ -232,6 +233,17 @@ class OracleTree:
         if r < 0:
             raise RuntimeError("oracle nearest traversal overflowed its 64-entry stack")
         return offsets, indices, dist
+
+
+def visit_counts(tree, mode, preds, k=0, kind=KIND_SPHERE):
+    """Mean (internal, leaf) node reads per query of the reference traversal:
+    mode 0 = nearest(k) over points [nq,3], mode 1 = spatial (kind)."""
+    p = _f32(preds, 3 if mode == 0 else (4 if kind == KIND_SPHERE else 6))
+    vi = ctypes.c_int64(0)
+    vl = ctypes.c_int64(0)
+    lib().abxo_visit_counts(*tree._tree_args(), int(mode), int(kind), _p(p), p.shape[0], int(k),
+                            ctypes.byref(vi), ctypes.byref(vl))
+    return vi.value / max(p.shape[0], 1), vl.value / max(p.shape[0], 1)
 
 
 def knn_brute(geom, queries, k, is_box=False):
