@@ -39,6 +39,8 @@ SIGNATURES = {
     "abx_last_error": (ctypes.c_char_p, []),
     "abx_version": (ctypes.c_char_p, []),
     "abx_device_errors": (_STATUS, [_P, ctypes.POINTER(ctypes.c_uint32)]),
+    "abx_tuning_set": (_STATUS, [ctypes.c_char_p, _I32]),
+    "abx_tuning_reset": (_STATUS, []),
     "abx_profiling_enable": (_STATUS, [_I32]),
     "abx_profiling_stage": (_STATUS, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)]),
     "abx_profiling_reset": (_STATUS, []),

@@ -18,13 +18,26 @@ abx_status morton64_codes(cudaStream_t s, abx_geometry kind, const float *d_g, i
 abx_status morton32_codes(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
                           const float *d_scene, uint32_t *d_codes, uint32_t *d_hist);
 
-// n >= 2.  d_tnodes may be null (then only the reference layout is written).
+// n >= 2.  d_tnodes and d_sorted (Morton-ordered leaf geometry, SortedLeaf)
+// may be null: scratch is used for them then.
 abx_status generate_hierarchy(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
                               const uint32_t *d_perm, const uint64_t *d_codes,
-                              LeafNode *d_leaves, InternalNode *d_internal, TNode *d_tnodes);
+                              LeafNode *d_leaves, InternalNode *d_internal, TNode *d_tnodes,
+                              float4 *d_sorted);
 
 abx_status single_leaf(cudaStream_t s, abx_geometry kind, const float *d_g,
-                       LeafNode *d_leaves, TNode *d_tnodes, float *d_bounds);
+                       LeafNode *d_leaves, TNode *d_tnodes, float4 *d_sorted, float *d_bounds);
+
+// Leaves per CTA of the block-local hierarchy climb.
+constexpr int kHierBlock = 512;
+
+// Largest subtree whose leaves a query may scan as one bucket, the flag of a
+// child slot's count field marking "Karras index = right end of the range",
+// and the default bucket limits of the query kernels.
+constexpr int kMaxBucket = 32;
+constexpr int kBucketRightEnd = 1 << 16;
+constexpr int kDefaultSpatialBucket = 8;
+constexpr int kDefaultNearestBucket = 1;
 
 // Tree view used by the query launchers.
 struct TreeView
@@ -32,6 +45,8 @@ struct TreeView
   const TNode *tnodes;
   int64_t n;
   const float *d_bounds; // 6 floats, the tree bounds
+  const float4 *sorted;  // leaf geometry in Morton order (SortedLeaf<kind>)
+  abx_geometry kind;     // ABX_POINT or ABX_BOX leaves
 };
 
 // Spatial query modes.

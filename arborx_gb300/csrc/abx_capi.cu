@@ -1,8 +1,11 @@
 // abx_capi.cu -- the extern "C" entry points of include/arborx_gb300.h:
 // tree construction pipeline, CRS query drivers, result objects, per-device
 // state and error reporting.
+#include <algorithm>
 #include <atomic>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -23,6 +26,7 @@ struct abx_bvh
   abx::LeafNode *leaves = nullptr;
   abx::InternalNode *internal = nullptr;
   abx::TNode *tnodes = nullptr;
+  float4 *sorted = nullptr;  // leaf geometry in Morton order (bucket scans)
   float *d_bounds = nullptr; // tree bounds on the device (6 floats)
   float *h_bounds = nullptr; // pinned copy, valid once `ready` completed
   cudaEvent_t ready = nullptr;
@@ -109,6 +113,26 @@ std::vector<StageRecord> g_prof;
 std::atomic<bool> g_prof_on{false};
 } // namespace
 
+namespace
+{
+std::mutex g_tuning_mutex;
+std::map<std::string, int> g_tuning;
+} // namespace
+
+int tuning_value(char const *name, int def)
+{
+  {
+    std::lock_guard<std::mutex> lock(g_tuning_mutex);
+    auto it = g_tuning.find(name);
+    if (it != g_tuning.end())
+      return it->second;
+  }
+  std::string env = std::string("ABX_TUNE_") + name;
+  if (char const *v = std::getenv(env.c_str()))
+    return std::atoi(v);
+  return def;
+}
+
 StageScope::StageScope(cudaStream_t s, char const *stage, int kernels)
     : stream_(s), stage_(stage), kernels_(kernels)
 {
@@ -180,6 +204,7 @@ void destroy_tree(abx_bvh *t)
   dfree(t->leaves, s);
   dfree(t->internal, s);
   dfree(t->tnodes, s);
+  dfree(t->sorted, s);
   dfree(t->d_bounds, s);
   if (t->h_bounds)
   {
@@ -217,10 +242,12 @@ abx_status build_tree(abx_bvh *t, const float *d_values)
     return ABX_SUCCESS;
   }
   ABX_CUDA_TRY(dmalloc_n(&t->leaves, n, s));
+  const int f4 = t->kind == ABX_BOX ? 2 : 1;
+  ABX_CUDA_TRY(dmalloc_n(&t->sorted, (size_t)n * f4, s));
   if (n == 1)
   {
     ABX_CUDA_TRY(dmalloc_n(&t->tnodes, 1, s));
-    ABX_TRY(single_leaf(s, t->kind, d_values, t->leaves, t->tnodes, t->d_bounds));
+    ABX_TRY(single_leaf(s, t->kind, d_values, t->leaves, t->tnodes, t->sorted, t->d_bounds));
   }
   else
   {
@@ -239,7 +266,7 @@ abx_status build_tree(abx_bvh *t, const float *d_values)
     ABX_TRY(morton64_codes(s, t->kind, d_values, n, t->d_bounds, codes.ptr, hist.ptr));
     ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, n, 8, hist.ptr));
     ABX_TRY(generate_hierarchy(s, t->kind, d_values, n, perm.ptr, codes.ptr, t->leaves,
-                               t->internal, t->tnodes));
+                               t->internal, t->tnodes, t->sorted));
   }
   ABX_CUDA_TRY(cudaMemcpyAsync(t->h_bounds, t->d_bounds, 6 * sizeof(float),
                                cudaMemcpyDeviceToHost, s));
@@ -260,7 +287,10 @@ abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
   return ABX_SUCCESS;
 }
 
-TreeView view_of(const abx_bvh *t) { return TreeView{t->tnodes, t->n, t->d_bounds}; }
+TreeView view_of(const abx_bvh *t)
+{
+  return TreeView{t->tnodes, t->n, t->d_bounds, t->sorted, t->kind};
+}
 
 } // namespace
 
@@ -294,6 +324,22 @@ abx_status abx_device_errors(void *stream, uint32_t *h_bits)
   DeviceState &ds = device_state();
   ABX_CUDA_TRY(cudaMemcpy(h_bits, ds.d_error, sizeof(unsigned), cudaMemcpyDeviceToHost));
   ABX_CUDA_TRY(cudaMemset(ds.d_error, 0, sizeof(unsigned)));
+  return ABX_SUCCESS;
+}
+
+abx_status abx_tuning_set(const char *name, int32_t value)
+{
+  if (!name)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_tuning_set: null name");
+  std::lock_guard<std::mutex> lock(g_tuning_mutex);
+  g_tuning[name] = value;
+  return ABX_SUCCESS;
+}
+
+abx_status abx_tuning_reset(void)
+{
+  std::lock_guard<std::mutex> lock(g_tuning_mutex);
+  g_tuning.clear();
   return ABX_SUCCESS;
 }
 
@@ -702,7 +748,7 @@ abx_status abx_generate_hierarchy(void *stream, abx_geometry kind, const float *
   device_state();
   return generate_hierarchy(as_stream(stream), kind, d_values, n, d_permutation, d_sorted_codes,
                             reinterpret_cast<LeafNode *>(d_leaves),
-                            reinterpret_cast<InternalNode *>(d_internal), nullptr);
+                            reinterpret_cast<InternalNode *>(d_internal), nullptr, nullptr);
 }
 
 abx_status abx_exclusive_scan_i32(void *stream, const int32_t *d_in, int64_t n, int32_t *d_out)

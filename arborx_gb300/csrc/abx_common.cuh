@@ -50,12 +50,18 @@ static_assert(sizeof(InternalNode) == 32, "reference internal node is 32 B");
 //   a = L.lo.x L.lo.y L.lo.z L.hi.x
 //   b = L.hi.y L.hi.z R.lo.x R.lo.y
 //   c = R.lo.z R.hi.x R.hi.y R.hi.z
-//   d = left ref, right ref, -, -
+//   d = left ref, right ref, left count, right count
 // A reference >= 0 is an internal node (index into the node array, Karras
-// numbering, root = 0); a reference < 0 is a leaf holding value ~ref.  For
-// point leaves the child box is the degenerate box [p, p]: the point-box
-// distance and intersection formulas then reduce bit-for-bit to the
-// point-point ones (closestPoint returns p exactly).
+// numbering, root = 0).  A reference < 0 is a leaf bucket of `count` leaves:
+// count 1 is a single leaf whose value is ~ref and whose bounding volume is
+// the child box stored in the node itself; count >= 2 covers the leaves at
+// sorted positions ~ref .. ~ref + count - 1, whose geometry and values are
+// stored contiguously in Morton order (the subtree of every node covering at
+// most `leaf size` leaves is collapsed into one bucket); count 0 marks an
+// absent child (one-leaf tree).  For point leaves a single leaf's box is the
+// degenerate box [p, p]: the point-box distance and intersection formulas
+// then reduce bit-for-bit to the point-point ones (closestPoint returns p
+// exactly).
 struct __align__(64) TNode
 {
   float4 a;
@@ -65,9 +71,9 @@ struct __align__(64) TNode
 };
 static_assert(sizeof(TNode) == 64, "traversal node is 64 B");
 
-__host__ __device__ __forceinline__ int leaf_ref(int value) { return ~value; }
-__host__ __device__ __forceinline__ bool is_leaf_ref(int ref) { return ref < 0; }
-__host__ __device__ __forceinline__ int leaf_value(int ref) { return ~ref; }
+__host__ __device__ __forceinline__ int bucket_ref(int start) { return ~start; }
+__host__ __device__ __forceinline__ bool is_bucket_ref(int ref) { return ref < 0; }
+__host__ __device__ __forceinline__ int bucket_start(int ref) { return ~ref; }
 
 struct Box3
 {
@@ -107,14 +113,14 @@ __device__ __forceinline__ void tnode_children(TNode const &t, Box3 &l, Box3 &r)
   r.hi[0] = t.c.y; r.hi[1] = t.c.z; r.hi[2] = t.c.w;
 }
 
-__device__ __forceinline__ TNode make_tnode(Box3 const &l, int lref, Box3 const &r,
-                                            int rref)
+__device__ __forceinline__ TNode make_tnode(Box3 const &l, int lref, int lcount, Box3 const &r,
+                                            int rref, int rcount)
 {
   TNode t;
   t.a = make_float4(l.lo[0], l.lo[1], l.lo[2], l.hi[0]);
   t.b = make_float4(l.hi[1], l.hi[2], r.lo[0], r.lo[1]);
   t.c = make_float4(r.lo[2], r.hi[0], r.hi[1], r.hi[2]);
-  t.d = make_int4(lref, rref, 0, 0);
+  t.d = make_int4(lref, rref, lcount, rcount);
   return t;
 }
 
@@ -322,6 +328,54 @@ __device__ __forceinline__ Box3 load_leaf_box(const float *g, int64_t i)
   return b;
 }
 
+// Leaf geometry in Morton order (the buckets' storage): points as
+// {x, y, z, value}; boxes as {lo.x, lo.y, lo.z, value}, {hi.x, hi.y, hi.z, 0}.
+template <int KIND>
+struct SortedLeaf;
+
+template <>
+struct SortedLeaf<0>
+{
+  static constexpr int kFloat4s = 1;
+  static __device__ __forceinline__ void store(float4 *s, int64_t i, Box3 const &b, int value)
+  {
+    s[i] = make_float4(b.lo[0], b.lo[1], b.lo[2], __int_as_float(value));
+  }
+  static __device__ __forceinline__ void load(const float4 *__restrict__ s, int64_t i, Box3 &b,
+                                              int &value)
+  {
+    const float4 v = __ldg(s + i);
+    b.lo[0] = b.hi[0] = v.x;
+    b.lo[1] = b.hi[1] = v.y;
+    b.lo[2] = b.hi[2] = v.z;
+    value = __float_as_int(v.w);
+  }
+};
+
+template <>
+struct SortedLeaf<1>
+{
+  static constexpr int kFloat4s = 2;
+  static __device__ __forceinline__ void store(float4 *s, int64_t i, Box3 const &b, int value)
+  {
+    s[2 * i] = make_float4(b.lo[0], b.lo[1], b.lo[2], __int_as_float(value));
+    s[2 * i + 1] = make_float4(b.hi[0], b.hi[1], b.hi[2], 0.f);
+  }
+  static __device__ __forceinline__ void load(const float4 *__restrict__ s, int64_t i, Box3 &b,
+                                              int &value)
+  {
+    const float4 u = __ldg(s + 2 * i);
+    const float4 v = __ldg(s + 2 * i + 1);
+    b.lo[0] = u.x;
+    b.lo[1] = u.y;
+    b.lo[2] = u.z;
+    b.hi[0] = v.x;
+    b.hi[1] = v.y;
+    b.hi[2] = v.z;
+    value = __float_as_int(u.w);
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Memory ordering
 // ---------------------------------------------------------------------------
@@ -334,6 +388,21 @@ __device__ __forceinline__ int atomic_cas_acq_rel(int *addr, int expected, int d
                : "l"(addr), "r"(expected), "r"(desired)
                : "memory");
   return old;
+}
+
+__device__ __forceinline__ int atomic_cas_relaxed(int *addr, int expected, int desired)
+{
+  int old;
+  asm volatile("atom.relaxed.gpu.global.cas.b32 %0, [%1], %2, %3;"
+               : "=r"(old)
+               : "l"(addr), "r"(expected), "r"(desired)
+               : "memory");
+  return old;
+}
+
+__device__ __forceinline__ void fence_acq_rel_gpu()
+{
+  asm volatile("fence.acq_rel.gpu;" ::: "memory");
 }
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *p)

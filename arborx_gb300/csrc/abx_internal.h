@@ -80,6 +80,10 @@ struct Scratch
       return abx_s_;                                                            \
   } while (0)
 
+// Tuning knob `name` (kernel variant, launch shape): the value set through
+// abx_tuning_set, else the environment variable ABX_TUNE_<name>, else `def`.
+int tuning_value(char const *name, int def);
+
 // Records a CUDA event pair around a kernel stage while profiling is enabled
 // (abx_profiling_enable); `kernels` is the number of launches in the stage.
 class StageScope

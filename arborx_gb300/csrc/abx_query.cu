@@ -1,17 +1,25 @@
-// abx_query.cu -- query traversal kernels over the 64-byte child-pair nodes.
+// abx_query.cu -- query traversal kernels over the 64-byte child-pair nodes
+// and the Morton-ordered leaf buckets.
 //
 //   k_spatial   intersects(Sphere | Box) predicates, one thread per query,
-//               depth-first with the left subtree first.  Hits come out in
-//               the same order as the reference's rope walk
-//               (TreeTraversal<Spatial>, ArborX_TreeTraversal.hpp:97-119);
-//               modes count / fill / buffered implement the CRS passes of
+//               depth-first with the left subtree first and the leaves of a
+//               bucket in Morton order.  Hits come out in the same order as
+//               the reference's rope walk (TreeTraversal<Spatial>,
+//               ArborX_TreeTraversal.hpp:97-119); modes count / fill /
+//               buffered implement the CRS passes of
 //               ArborX_CrsGraphWrapperImpl.hpp:148-323.
-//   k_nearest   nearest(Point, k) with the k best (distance, index) pairs in
+//   k_nearest   nearest(Point, k) keeping the k best (distance, index) keys in
 //               registers (k <= 32), closer child first, pruning by the k-th
 //               distance (TreeTraversal<Nearest>, ArborX_TreeTraversal.hpp:
 //               180-335, with the heap replaced by a sorted register list).
 //   k_nearest_large  the same for k > 32 with a bounded max-heap kept in the
 //               query's slice of the output arrays (misc/ArborX_Heap.hpp).
+//
+// Distances are compared squared: sqrt_rn is monotone, so a squared distance
+// s passes "distance <= r" exactly when s <= sq_threshold(r), the largest
+// float whose correctly rounded square root is <= r.  Square roots are taken
+// only for candidates that can enter a result, which keeps every decision
+// and every reported distance bit-identical to the sqrt-per-test formula.
 #include <algorithm>
 #include <cmath>
 
@@ -31,25 +39,70 @@ __device__ __forceinline__ TNode load_tnode(const TNode *__restrict__ nodes, int
   t.a = __ldg(p);
   t.b = __ldg(p + 1);
   t.c = __ldg(p + 2);
-  float4 d = __ldg(p + 3);
-  t.d = make_int4(__float_as_int(d.x), __float_as_int(d.y), 0, 0);
+  const float4 d = __ldg(p + 3);
+  t.d = make_int4(__float_as_int(d.x), __float_as_int(d.y), __float_as_int(d.z),
+                  __float_as_int(d.w));
   return t;
 }
 
+// Largest float s with sqrt_rn(s) <= r, for r >= 0 (+inf for r = +inf).
+// RN(r * r) lies within a couple of ulps of the answer (sqrt_rn(RN(r*r)) = r
+// without overflow or underflow), so the two bounded walks always finish.
+__device__ __forceinline__ float sq_threshold(float r)
+{
+  if (!(r < INFINITY))
+    return INFINITY;
+  float t = __fmul_rn(r, r);
+#pragma unroll 1
+  for (int i = 0; i < 8 && __fsqrt_rn(t) > r; ++i)
+    t = __int_as_float(__float_as_int(t) - 1);
+#pragma unroll 1
+  for (int i = 0; i < 8; ++i)
+  {
+    const float u = __int_as_float(__float_as_int(t) + 1);
+    if (__fsqrt_rn(u) <= r)
+      t = u;
+    else
+      break;
+  }
+  return t;
+}
+
+// Squared distance from a point to a leaf's bounding volume.
+template <int KIND>
+__device__ __forceinline__ float leaf_dist2(float qx, float qy, float qz, Box3 const &b)
+{
+  if (KIND == 0)
+    return dist2_pp(qx, qy, qz, b.lo[0], b.lo[1], b.lo[2]);
+  return dist2_pb(qx, qy, qz, b);
+}
+
+// intersects(Sphere, .) with the radius test done on squared distances:
+// sphere-box (ArborX_Intersects.hpp:83-92) and, for point leaves,
+// sphere-point (:106-115).
 struct SpherePred
 {
-  float cx, cy, cz, r;
-  __device__ __forceinline__ bool test(Box3 const &b) const
+  float cx, cy, cz, r, r2;
+  __device__ __forceinline__ bool test(Box3 const &b) const { return dist2_pb(cx, cy, cz, b) <= r2; }
+  template <int KIND>
+  __device__ __forceinline__ bool test_leaf(Box3 const &b) const
   {
-    // intersects(Sphere, Box) (ArborX_Intersects.hpp:83-92)
-    return dist_pb(cx, cy, cz, b) <= r;
+    return leaf_dist2<KIND>(cx, cy, cz, b) <= r2;
   }
 };
 
+// intersects(Box, .): box-box (ArborX_Intersects.hpp:52-65), for point leaves
+// point-box through reverse dispatch (:68-80; the degenerate box [p, p] gives
+// the same comparisons).
 struct BoxPred
 {
   Box3 b;
   __device__ __forceinline__ bool test(Box3 const &o) const { return isect_bb(b, o); }
+  template <int KIND>
+  __device__ __forceinline__ bool test_leaf(Box3 const &o) const
+  {
+    return isect_bb(b, o);
+  }
 };
 
 template <int PRED>
@@ -57,17 +110,18 @@ struct PredOf;
 template <>
 struct PredOf<ABX_SPHERE>
 {
-  using type = SpherePred;
   static __device__ __forceinline__ SpherePred load(const float *p, int64_t q)
   {
     const float *s = p + 4 * q;
-    return SpherePred{__ldg(s), __ldg(s + 1), __ldg(s + 2), __ldg(s + 3)};
+    SpherePred sp{__ldg(s), __ldg(s + 1), __ldg(s + 2), __ldg(s + 3), 0.f};
+    // a negative radius matches nothing (sqrt_rn(s) >= 0 > r)
+    sp.r2 = sp.r >= 0.f ? sq_threshold(sp.r) : -1.f;
+    return sp;
   }
 };
 template <>
 struct PredOf<ABX_BOX>
 {
-  using type = BoxPred;
   static __device__ __forceinline__ BoxPred load(const float *p, int64_t q)
   {
     const float *s = p + 6 * q;
@@ -82,11 +136,44 @@ struct PredOf<ABX_BOX>
   }
 };
 
-template <int PRED, int MODE>
+// ---------------------------------------------------------------------------
+// Spatial
+// ---------------------------------------------------------------------------
+
+// How a traversal handles a child slot (ref, count field): descend into an
+// internal node, take a single leaf (its box is the child box), or scan the
+// leaves of a small internal subtree from the Morton-ordered copy.
+enum ChildKind
+{
+  kDescend = 0,
+  kLeaf = 1,
+  kScan = 2,
+  kNone = 3
+};
+
+template <bool SCAN>
+__device__ __forceinline__ ChildKind child_kind(int ref, int cf, int bucket, int &start, int &cnt)
+{
+  if (is_bucket_ref(ref))
+    return cf == 0 ? kNone : kLeaf;
+  if (!SCAN)
+    return kDescend;
+  const int c = cf & 0xffff;
+  if (c >= 2 && c <= bucket)
+  {
+    cnt = c;
+    start = (cf & kBucketRightEnd) ? ref - c + 1 : ref;
+    return kScan;
+  }
+  return kDescend;
+}
+
+template <int PRED, int MODE, int KIND>
 __global__ void __launch_bounds__(kQueryThreads)
-    k_spatial(const TNode *__restrict__ nodes, int64_t n, const float *__restrict__ preds,
-              int64_t nq, const uint32_t *__restrict__ perm, int32_t *__restrict__ counts,
-              const int32_t *__restrict__ offsets, int32_t *__restrict__ out, int32_t buffer,
+    k_spatial(const TNode *__restrict__ nodes, const float4 *__restrict__ sorted, int64_t n,
+              const float *__restrict__ preds, int64_t nq, const uint32_t *__restrict__ perm,
+              int32_t *__restrict__ counts, const int32_t *__restrict__ offsets,
+              int32_t *__restrict__ out, int32_t buffer, int bucket,
               unsigned *__restrict__ overflow, unsigned *__restrict__ err)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -105,84 +192,95 @@ __global__ void __launch_bounds__(kQueryThreads)
     cap = buffer;
   }
   int32_t count = 0;
-  auto emit = [&](int ref) {
-    const int v = leaf_value(ref);
+  auto emit = [&](int v) {
     if (MODE == kFill)
       dst[count] = v;
     if (MODE == kBuffered && count < cap)
       dst[count] = v;
     ++count;
   };
+  // the leaves of a small subtree, in Morton (= rope walk) order
+  auto scan = [&](int start, int cnt) {
+    for (int j = 0; j < cnt; ++j)
+    {
+      Box3 b;
+      int v;
+      SortedLeaf<KIND>::load(sorted, start + j, b, v);
+      if (pred.template test_leaf<KIND>(b))
+        emit(v);
+    }
+  };
+  // a child that passed its box test; returns true when it is to be
+  // descended into
+  auto visit = [&](int ref, int cf) -> bool {
+    int start = 0, cnt = 0;
+    const ChildKind k = child_kind<true>(ref, cf, bucket, start, cnt);
+    if (k == kLeaf)
+      emit(bucket_start(ref));
+    else if (k == kScan)
+      scan(start, cnt);
+    return k == kDescend;
+  };
 
-  if (n == 1)
+  int sref[kStackDepth];
+  int scf[kStackDepth];
+  int sp = 0;
+  int node = 0;
+  const int64_t num_nodes = n > 1 ? n - 1 : 1;
+  int64_t budget = num_nodes; // a depth-first walk visits each node at most once
+  while (true)
   {
-    TNode tn = load_tnode(nodes, 0);
+    if (--budget < 0 || (uint64_t)node >= (uint64_t)num_nodes)
+    {
+      raise_error(err, ABX_DEVERR_INTERNAL);
+      break;
+    }
+    const TNode tn = load_tnode(nodes, node);
     Box3 l, r;
     tnode_children(tn, l, r);
-    if (pred.test(l))
-      emit(tn.d.x);
-  }
-  else
-  {
-    int stack[kStackDepth];
-    int sp = 0;
-    int node = 0;
-    // a depth-first walk visits each of the n - 1 internal nodes at most once
-    int64_t budget = n;
-    while (true)
+    const int lref = tn.d.x, rref = tn.d.y;
+    const int lcf = tn.d.z, rcf = tn.d.w;
+    const bool rnone = is_bucket_ref(rref) && rcf == 0; // one-leaf tree
+    const bool hl = pred.test(l);
+    const bool hr = !rnone && pred.test(r);
+    bool has_next = false;
+    int next = 0;
+    if (hl && visit(lref, lcf))
     {
-      if (--budget < 0 || (uint64_t)node >= (uint64_t)(n - 1))
+      next = lref;
+      has_next = true;
+    }
+    if (hr)
+    {
+      if (!has_next)
       {
-        raise_error(err, ABX_DEVERR_INTERNAL);
-        break;
-      }
-      const TNode tn = load_tnode(nodes, node);
-      Box3 l, r;
-      tnode_children(tn, l, r);
-      const int lref = tn.d.x, rref = tn.d.y;
-      const bool hl = pred.test(l);
-      const bool hr = pred.test(r);
-      bool has_next = false;
-      int next = 0;
-      if (hl)
-      {
-        if (is_leaf_ref(lref))
-          emit(lref);
-        else
-        {
-          next = lref;
-          has_next = true;
-        }
-      }
-      if (hr)
-      {
-        if (!has_next && is_leaf_ref(rref))
-          emit(rref);
-        else if (!has_next)
+        if (visit(rref, rcf))
         {
           next = rref;
           has_next = true;
         }
-        else if (sp < kStackDepth)
-          stack[sp++] = rref;
-        else
-          raise_error(err, ABX_DEVERR_STACK_OVERFLOW);
       }
-      while (!has_next && sp > 0)
+      else if (sp < kStackDepth)
       {
-        const int ref = stack[--sp];
-        if (is_leaf_ref(ref))
-          emit(ref);
-        else
-        {
-          next = ref;
-          has_next = true;
-        }
+        sref[sp] = rref;
+        scf[sp] = rcf;
+        ++sp;
       }
-      if (!has_next)
-        break;
-      node = next;
+      else
+        raise_error(err, ABX_DEVERR_STACK_OVERFLOW);
     }
+    while (!has_next && sp > 0)
+    {
+      --sp;
+      if (visit(sref[sp], scf[sp]))
+      {
+        next = sref[sp];
+        has_next = true;
+      }
+    }
+    if (!has_next)
+      break;
+    node = next;
   }
   if (MODE != kFill)
     counts[q] = count;
@@ -205,151 +303,204 @@ __global__ void k_compact(const int32_t *__restrict__ tmp, int64_t nq, int32_t b
     out[o + j] = src[j];
 }
 
-// (distance, index) order of the k-nearest result.
-__device__ __forceinline__ bool pair_lt(float da, int ia, float db, int ib)
-{
-  return da < db || (da == db && ia < ib);
-}
+// ---------------------------------------------------------------------------
+// Nearest
+// ---------------------------------------------------------------------------
 
-template <int K>
-__device__ __forceinline__ void list_insert(float (&bd)[K], int (&bi)[K], float d, int v)
+// A k-nearest candidate as one 64-bit key: the distance's bit pattern (a
+// non-negative float, so unsigned order = numeric order) above the value + 1.
+// Unsigned key order is exactly the (distance, index) order; 0 sorts before
+// every candidate and ~0 after every candidate.
+constexpr uint64_t kKeyEmpty = ~0ull;
+
+__device__ __forceinline__ uint64_t knn_key(float d, int value)
 {
-  bool done = false;
+  return ((uint64_t)__float_as_uint(d) << 32) | (uint32_t)(value + 1);
+}
+__device__ __forceinline__ float key_dist(uint64_t k) { return __uint_as_float((uint32_t)(k >> 32)); }
+__device__ __forceinline__ int key_value(uint64_t k) { return (int)(uint32_t)k - 1; }
+
+// Insert c into the ascending list (precondition: c < key[K-1]).
+template <int K>
+__device__ __forceinline__ void list_insert(uint64_t (&key)[K], uint64_t c)
+{
+  bool lt[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    lt[j] = c < key[j];
 #pragma unroll
   for (int j = K - 1; j >= 1; --j)
-  {
-    const bool move = !done && pair_lt(d, v, bd[j - 1], bi[j - 1]);
-    const bool place = !done && !move;
-    bd[j] = move ? bd[j - 1] : (place ? d : bd[j]);
-    bi[j] = move ? bi[j - 1] : (place ? v : bi[j]);
-    done = done || place;
-  }
-  if (!done)
-  {
-    bd[0] = d;
-    bi[0] = v;
-  }
+    key[j] = lt[j - 1] ? key[j - 1] : (lt[j] ? c : key[j]);
+  key[0] = lt[0] ? c : key[0];
 }
 
-// The list keeps K slots; the first K - k hold (-inf, -1) sentinels that no
-// candidate displaces, so the k-th best is always slot K - 1 (static index).
-template <int K>
+struct KnnTask
+{
+  int64_t q;
+  int k;
+  int kk;
+  int64_t base;
+};
+
+__device__ __forceinline__ KnnTask knn_task(int64_t t, int64_t n, int64_t nq,
+                                            const uint32_t *__restrict__ perm,
+                                            const int32_t *__restrict__ kq, int32_t k_all,
+                                            const int32_t *__restrict__ offsets,
+                                            int32_t *__restrict__ offsets_out)
+{
+  KnnTask task;
+  task.q = perm ? (int64_t)__ldg(perm + t) : t;
+  const int k = kq ? __ldg(kq + task.q) : k_all;
+  task.k = k < 0 ? 0 : k;
+  task.kk = (int)((int64_t)task.k < n ? (int64_t)task.k : n);
+  task.base = offsets ? (int64_t)__ldg(offsets + task.q) : task.q * (int64_t)task.kk;
+  if (offsets_out)
+  {
+    offsets_out[task.q] = (int32_t)task.base;
+    if (task.q == nq - 1)
+      offsets_out[nq] = (int32_t)(task.base + task.kk);
+  }
+  return task;
+}
+
+// One query per thread.  The list keeps K slots; the first K - k hold the
+// key 0 (never displaced), so the k-th best is always slot K - 1.  thr is
+// sq_threshold of the k-th best distance (+inf until the list is full): a
+// node or leaf whose squared distance s satisfies s <= thr can still hold a
+// better candidate.  Buckets are scanned as soon as their box passes; of two
+// passing internal children the closer is visited first and the other waits
+// on the stack with its squared distance.
+template <int K, int KIND, bool SCAN>
 __global__ void __launch_bounds__(kQueryThreads)
-    k_nearest(const TNode *__restrict__ nodes, int64_t n, const float *__restrict__ queries,
-              int64_t nq, const uint32_t *__restrict__ perm, const int32_t *__restrict__ kq,
-              int32_t k_all, const int32_t *__restrict__ offsets,
+    k_nearest(const TNode *__restrict__ nodes, const float4 *__restrict__ sorted, int64_t n,
+              const float *__restrict__ queries, int64_t nq, const uint32_t *__restrict__ perm,
+              const int32_t *__restrict__ kq, int32_t k_all, const int32_t *__restrict__ offsets,
               int32_t *__restrict__ offsets_out, int32_t *__restrict__ out_idx,
-              float *__restrict__ out_dist, unsigned *__restrict__ err)
+              float *__restrict__ out_dist, int bucket, unsigned *__restrict__ err)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nq)
     return;
-  const int64_t q = perm ? (int64_t)__ldg(perm + t) : t;
-  int k = kq ? __ldg(kq + q) : k_all;
-  k = k < 0 ? 0 : k;
-  const int kk = (int)((int64_t)k < n ? (int64_t)k : n);
-  const int64_t base = offsets ? (int64_t)__ldg(offsets + q) : q * (int64_t)kk;
-  if (offsets_out)
-  {
-    offsets_out[q] = (int32_t)base;
-    if (q == nq - 1)
-      offsets_out[nq] = (int32_t)(base + kk);
-  }
-  if (kk == 0)
+  const KnnTask task = knn_task(t, n, nq, perm, kq, k_all, offsets, offsets_out);
+  if (task.kk == 0)
     return;
-
-  float bd[K];
-  int bi[K];
-  const int first = K - k;
+  uint64_t key[K];
+  const int first = K - task.k;
 #pragma unroll
   for (int j = 0; j < K; ++j)
-  {
-    bd[j] = j < first ? -INFINITY : INFINITY;
-    bi[j] = j < first ? -1 : 0x7fffffff;
-  }
-  const float qx = __ldg(queries + 3 * q), qy = __ldg(queries + 3 * q + 1),
-              qz = __ldg(queries + 3 * q + 2);
+    key[j] = j < first ? 0ull : kKeyEmpty;
+  float thr = INFINITY;
+  const float qx = __ldg(queries + 3 * task.q), qy = __ldg(queries + 3 * task.q + 1),
+              qz = __ldg(queries + 3 * task.q + 2);
 
-  if (n == 1)
+  auto offer = [&](float s, int v) {
+    const uint64_t c = knn_key(__fsqrt_rn(s), v);
+    if (c < key[K - 1])
+    {
+      list_insert<K>(key, c);
+      if (key[K - 1] != kKeyEmpty)
+        thr = sq_threshold(key_dist(key[K - 1]));
+    }
+  };
+  // s_box: squared distance to the bucket's box (for a single leaf, its
+  // own squared distance)
+  // a child whose box passed (squared distance s_box); returns true when it
+  // is an internal node to descend into
+  auto visit = [&](int ref, int cf, float s_box) -> bool {
+    int start = 0, cnt = 0;
+    const ChildKind kind = child_kind<SCAN>(ref, cf, bucket, start, cnt);
+    if (kind == kLeaf)
+      offer(s_box, bucket_start(ref));
+    else if (SCAN && kind == kScan)
+    {
+      for (int j = 0; j < cnt; ++j)
+      {
+        Box3 b;
+        int v;
+        SortedLeaf<KIND>::load(sorted, start + j, b, v);
+        const float s = leaf_dist2<KIND>(qx, qy, qz, b);
+        if (s <= thr)
+          offer(s, v);
+      }
+    }
+    return kind == kDescend;
+  };
+
+  int sref[kStackDepth];
+  float sdist[kStackDepth];
+  int sp = 0;
+  int node = 0;
+  const int64_t num_nodes = n > 1 ? n - 1 : 1;
+  int64_t budget = num_nodes;
+  while (true)
   {
-    TNode tn = load_tnode(nodes, 0);
+    if (--budget < 0 || (uint64_t)node >= (uint64_t)num_nodes)
+    {
+      raise_error(err, ABX_DEVERR_INTERNAL);
+      break;
+    }
+    const TNode tn = load_tnode(nodes, node);
     Box3 l, r;
     tnode_children(tn, l, r);
-    list_insert<K>(bd, bi, dist_pb(qx, qy, qz, l), leaf_value(tn.d.x));
-  }
-  else
-  {
-    int sref[kStackDepth];
-    float sdist[kStackDepth];
-    int sp = 0;
-    int node = 0;
-    int64_t budget = n; // each internal node is visited at most once
-    while (true)
+    const int lref = tn.d.x, rref = tn.d.y;
+    const bool rnone = is_bucket_ref(rref) && tn.d.w == 0; // one-leaf tree: no right child
+    const float sl = dist2_pb(qx, qy, qz, l);
+    const float sr = rnone ? INFINITY : dist2_pb(qx, qy, qz, r);
+    // leaves and scanned subtrees first (they may tighten thr), then the
+    // internal children that still pass
+    bool dl = sl <= thr && visit(lref, tn.d.z, sl);
+    bool dr = sr <= thr && visit(rref, tn.d.w, sr);
+    const bool gl = dl && sl <= thr;
+    const bool gr = dr && sr <= thr;
+    if (gl && gr)
     {
-      if (--budget < 0 || (uint64_t)node >= (uint64_t)(n - 1))
+      const bool left_first = sl <= sr;
+      node = left_first ? lref : rref;
+      if (sp < kStackDepth)
       {
-        raise_error(err, ABX_DEVERR_INTERNAL);
+        sref[sp] = left_first ? rref : lref;
+        sdist[sp] = left_first ? sr : sl;
+        ++sp;
+      }
+      else
+        raise_error(err, ABX_DEVERR_STACK_OVERFLOW);
+      continue;
+    }
+    if (gl || gr)
+    {
+      node = gl ? lref : rref;
+      continue;
+    }
+    bool found = false;
+    while (sp > 0)
+    {
+      --sp;
+      if (sdist[sp] <= thr)
+      {
+        node = sref[sp];
+        found = true;
         break;
       }
-      const TNode tn = load_tnode(nodes, node);
-      Box3 l, r;
-      tnode_children(tn, l, r);
-      const int lref = tn.d.x, rref = tn.d.y;
-      const float dl = dist_pb(qx, qy, qz, l);
-      const float dr = dist_pb(qx, qy, qz, r);
-      const bool ll = is_leaf_ref(lref), rl = is_leaf_ref(rref);
-      if (ll && pair_lt(dl, leaf_value(lref), bd[K - 1], bi[K - 1]))
-        list_insert<K>(bd, bi, dl, leaf_value(lref));
-      if (rl && pair_lt(dr, leaf_value(rref), bd[K - 1], bi[K - 1]))
-        list_insert<K>(bd, bi, dr, leaf_value(rref));
-      const float rad = bd[K - 1];
-      const bool gl = !ll && dl <= rad;
-      const bool gr = !rl && dr <= rad;
-      if (gl && gr)
-      {
-        const bool left_first = dl <= dr;
-        node = left_first ? lref : rref;
-        if (sp < kStackDepth)
-        {
-          sref[sp] = left_first ? rref : lref;
-          sdist[sp] = left_first ? dr : dl;
-          ++sp;
-        }
-        else
-          raise_error(err, ABX_DEVERR_STACK_OVERFLOW);
-      }
-      else if (gl)
-        node = lref;
-      else if (gr)
-        node = rref;
-      else
-      {
-        bool found = false;
-        while (sp > 0)
-        {
-          --sp;
-          if (sdist[sp] <= bd[K - 1])
-          {
-            node = sref[sp];
-            found = true;
-            break;
-          }
-        }
-        if (!found)
-          break;
-      }
     }
+    if (!found)
+      break;
   }
 #pragma unroll
   for (int j = 0; j < K; ++j)
   {
-    if (j >= first && j < first + kk)
+    if (j >= first && j < first + task.kk)
     {
-      out_idx[base + (j - first)] = bi[j];
+      out_idx[task.base + (j - first)] = key_value(key[j]);
       if (out_dist)
-        out_dist[base + (j - first)] = bd[j];
+        out_dist[task.base + (j - first)] = key_dist(key[j]);
     }
   }
+}
+
+// (distance, index) order of the k-nearest result.
+__device__ __forceinline__ bool pair_lt(float da, int ia, float db, int ib)
+{
+  return da < db || (da == db && ia < ib);
 }
 
 // Bounded max-heap on (distance, index) in global memory: the farthest of
@@ -379,7 +530,7 @@ __device__ void heap_push(float *hd, int *hi, int &size, float d, int v)
   int pos = size++;
   while (pos > 0)
   {
-    int parent = (pos - 1) / 2;
+    const int parent = (pos - 1) / 2;
     if (!pair_lt(hd[parent], hi[parent], d, v))
       break;
     hd[pos] = hd[parent];
@@ -390,121 +541,124 @@ __device__ void heap_push(float *hd, int *hi, int &size, float d, int v)
   hi[pos] = v;
 }
 
-__device__ void heap_offer(float *hd, int *hi, int &size, int k, float d, int v)
-{
-  if (size < k)
-    heap_push(hd, hi, size, d, v);
-  else if (pair_lt(d, v, hd[0], hi[0]))
-    heap_sift_down(hd, hi, 0, size, d, v);
-}
-
+template <int KIND>
 __global__ void __launch_bounds__(kQueryThreads)
-    k_nearest_large(const TNode *__restrict__ nodes, int64_t n,
-                    const float *__restrict__ queries, int64_t nq,
+    k_nearest_large(const TNode *__restrict__ nodes, const float4 *__restrict__ sorted,
+                    int64_t n, const float *__restrict__ queries, int64_t nq,
                     const uint32_t *__restrict__ perm, const int32_t *__restrict__ kq,
                     int32_t k_all, const int32_t *__restrict__ offsets,
                     int32_t *__restrict__ offsets_out, int32_t *__restrict__ out_idx,
-                    float *__restrict__ out_dist, unsigned *__restrict__ err)
+                    float *__restrict__ out_dist, int bucket, unsigned *__restrict__ err)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nq)
     return;
-  const int64_t q = perm ? (int64_t)__ldg(perm + t) : t;
-  int k = kq ? __ldg(kq + q) : k_all;
-  k = k < 0 ? 0 : k;
-  const int kk = (int)((int64_t)k < n ? (int64_t)k : n);
-  const int64_t base = offsets ? (int64_t)__ldg(offsets + q) : q * (int64_t)kk;
-  if (offsets_out)
-  {
-    offsets_out[q] = (int32_t)base;
-    if (q == nq - 1)
-      offsets_out[nq] = (int32_t)(base + kk);
-  }
+  const KnnTask task = knn_task(t, n, nq, perm, kq, k_all, offsets, offsets_out);
+  const int kk = task.kk;
   if (kk == 0)
     return;
-  float *hd = out_dist + base;
-  int *hi = out_idx + base;
+  float *hd = out_dist + task.base;
+  int *hi = out_idx + task.base;
   int size = 0;
-  const float qx = queries[3 * q], qy = queries[3 * q + 1], qz = queries[3 * q + 2];
-  if (n == 1)
-  {
-    TNode tn = load_tnode(nodes, 0);
-    Box3 l, r;
-    tnode_children(tn, l, r);
-    heap_offer(hd, hi, size, kk, dist_pb(qx, qy, qz, l), leaf_value(tn.d.x));
-  }
-  else
-  {
-    int sref[kStackDepth];
-    float sdist[kStackDepth];
-    int sp = 0;
-    int node = 0;
-    int64_t budget = n; // each internal node is visited at most once
-    while (true)
+  float thr = INFINITY;
+  const float qx = queries[3 * task.q], qy = queries[3 * task.q + 1], qz = queries[3 * task.q + 2];
+  auto offer = [&](float s, int v) {
+    const float d = __fsqrt_rn(s);
+    if (size < kk)
+      heap_push(hd, hi, size, d, v);
+    else if (pair_lt(d, v, hd[0], hi[0]))
+      heap_sift_down(hd, hi, 0, size, d, v);
+    else
+      return;
+    if (size == kk)
+      thr = sq_threshold(hd[0]);
+  };
+  // a child whose box passed (squared distance s_box); returns true when it
+  // is an internal node to descend into
+  auto visit = [&](int ref, int cf, float s_box) -> bool {
+    int start = 0, cnt = 0;
+    const ChildKind kind = child_kind<true>(ref, cf, bucket, start, cnt);
+    if (kind == kLeaf)
+      offer(s_box, bucket_start(ref));
+    else if (kind == kScan)
     {
-      if (--budget < 0 || (uint64_t)node >= (uint64_t)(n - 1))
+      for (int j = 0; j < cnt; ++j)
       {
-        raise_error(err, ABX_DEVERR_INTERNAL);
-        break;
-      }
-      const TNode tn = load_tnode(nodes, node);
-      Box3 l, r;
-      tnode_children(tn, l, r);
-      const int lref = tn.d.x, rref = tn.d.y;
-      const float dl = dist_pb(qx, qy, qz, l);
-      const float dr = dist_pb(qx, qy, qz, r);
-      const bool ll = is_leaf_ref(lref), rl = is_leaf_ref(rref);
-      if (ll)
-        heap_offer(hd, hi, size, kk, dl, leaf_value(lref));
-      if (rl)
-        heap_offer(hd, hi, size, kk, dr, leaf_value(rref));
-      const float rad = size == kk ? hd[0] : INFINITY;
-      const bool gl = !ll && dl <= rad;
-      const bool gr = !rl && dr <= rad;
-      if (gl && gr)
-      {
-        const bool left_first = dl <= dr;
-        node = left_first ? lref : rref;
-        if (sp < kStackDepth)
-        {
-          sref[sp] = left_first ? rref : lref;
-          sdist[sp] = left_first ? dr : dl;
-          ++sp;
-        }
-        else
-          raise_error(err, ABX_DEVERR_STACK_OVERFLOW);
-      }
-      else if (gl)
-        node = lref;
-      else if (gr)
-        node = rref;
-      else
-      {
-        bool found = false;
-        while (sp > 0)
-        {
-          --sp;
-          const float radn = size == kk ? hd[0] : INFINITY;
-          if (sdist[sp] <= radn)
-          {
-            node = sref[sp];
-            found = true;
-            break;
-          }
-        }
-        if (!found)
-          break;
+        Box3 b;
+        int v;
+        SortedLeaf<KIND>::load(sorted, start + j, b, v);
+        const float s = leaf_dist2<KIND>(qx, qy, qz, b);
+        if (s <= thr)
+          offer(s, v);
       }
     }
+    return kind == kDescend;
+  };
+  int sref[kStackDepth];
+  float sdist[kStackDepth];
+  int sp = 0;
+  int node = 0;
+  const int64_t num_nodes = n > 1 ? n - 1 : 1;
+  int64_t budget = num_nodes;
+  while (true)
+  {
+    if (--budget < 0 || (uint64_t)node >= (uint64_t)num_nodes)
+    {
+      raise_error(err, ABX_DEVERR_INTERNAL);
+      break;
+    }
+    const TNode tn = load_tnode(nodes, node);
+    Box3 l, r;
+    tnode_children(tn, l, r);
+    const int lref = tn.d.x, rref = tn.d.y;
+    const bool rnone = is_bucket_ref(rref) && tn.d.w == 0; // one-leaf tree: no right child
+    const float sl = dist2_pb(qx, qy, qz, l);
+    const float sr = rnone ? INFINITY : dist2_pb(qx, qy, qz, r);
+    // leaves and scanned subtrees first (they may tighten thr), then the
+    // internal children that still pass
+    bool dl = sl <= thr && visit(lref, tn.d.z, sl);
+    bool dr = sr <= thr && visit(rref, tn.d.w, sr);
+    const bool gl = dl && sl <= thr;
+    const bool gr = dr && sr <= thr;
+    if (gl && gr)
+    {
+      const bool left_first = sl <= sr;
+      node = left_first ? lref : rref;
+      if (sp < kStackDepth)
+      {
+        sref[sp] = left_first ? rref : lref;
+        sdist[sp] = left_first ? sr : sl;
+        ++sp;
+      }
+      else
+        raise_error(err, ABX_DEVERR_STACK_OVERFLOW);
+      continue;
+    }
+    if (gl || gr)
+    {
+      node = gl ? lref : rref;
+      continue;
+    }
+    bool found = false;
+    while (sp > 0)
+    {
+      --sp;
+      if (sdist[sp] <= thr)
+      {
+        node = sref[sp];
+        found = true;
+        break;
+      }
+    }
+    if (!found)
+      break;
   }
   // heap sort into ascending (distance, index) order
   for (int len = size; len > 1; --len)
   {
-    float d0 = hd[0];
-    int i0 = hi[0];
-    float dl = hd[len - 1];
-    int il = hi[len - 1];
-    heap_sift_down(hd, hi, 0, len - 1, dl, il);
+    const float d0 = hd[0];
+    const int i0 = hi[0];
+    heap_sift_down(hd, hi, 0, len - 1, hd[len - 1], hi[len - 1]);
     hd[len - 1] = d0;
     hi[len - 1] = i0;
   }
@@ -513,7 +667,7 @@ __global__ void __launch_bounds__(kQueryThreads)
 __global__ void k_knn_counts(const int32_t *__restrict__ kq, int64_t nq, int64_t n,
                              int32_t *__restrict__ counts, int32_t *__restrict__ kmax)
 {
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int32_t m = 0;
   if (i < nq)
   {
@@ -529,24 +683,87 @@ __global__ void k_knn_counts(const int32_t *__restrict__ kq, int64_t nq, int64_t
     atomicMax(kmax, m);
 }
 
-template <int PRED>
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+
+template <int PRED, int KIND>
 abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, const float *d_preds,
                             int64_t nq, const uint32_t *d_perm, SpatialMode mode,
                             int32_t *d_counts, const int32_t *d_offsets, int32_t *d_out,
                             int32_t buffer, unsigned *d_overflow)
 {
   unsigned *err = device_state().d_error;
-  unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
-  StageScope scope(s, "spatial", 1);
+  const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
+  const int bucket =
+      std::max(1, std::min(kMaxBucket, tuning_value("SPATIAL_BUCKET", kDefaultSpatialBucket)));
+#define ABX_SPATIAL(M)                                                                      \
+  k_spatial<PRED, M, KIND><<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.sorted, t.n, d_preds, \
+                                                            nq, d_perm, d_counts, d_offsets,  \
+                                                            d_out, buffer, bucket, d_overflow, \
+                                                            err)
   if (mode == kCount)
-    k_spatial<PRED, kCount><<<blocks, kQueryThreads, 0, s>>>(
-        t.tnodes, t.n, d_preds, nq, d_perm, d_counts, d_offsets, d_out, buffer, d_overflow, err);
+    ABX_SPATIAL(kCount);
   else if (mode == kFill)
-    k_spatial<PRED, kFill><<<blocks, kQueryThreads, 0, s>>>(
-        t.tnodes, t.n, d_preds, nq, d_perm, d_counts, d_offsets, d_out, buffer, d_overflow, err);
+    ABX_SPATIAL(kFill);
   else
-    k_spatial<PRED, kBuffered><<<blocks, kQueryThreads, 0, s>>>(
-        t.tnodes, t.n, d_preds, nq, d_perm, d_counts, d_offsets, d_out, buffer, d_overflow, err);
+    ABX_SPATIAL(kBuffered);
+#undef ABX_SPATIAL
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
+
+template <int K, int KIND>
+abx_status nearest_k(cudaStream_t s, TreeView const &t, const float *d_queries, int64_t nq,
+                     const uint32_t *d_perm, const int32_t *d_k, int32_t k,
+                     const int32_t *d_offsets, int32_t *d_offsets_out, int32_t *d_idx,
+                     float *d_dist, unsigned *err)
+{
+  const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
+  const int bucket =
+      std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
+  if (bucket >= 2)
+    k_nearest<K, KIND, true><<<blocks, kQueryThreads, 0, s>>>(
+        t.tnodes, t.sorted, t.n, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, d_idx,
+        d_dist, bucket, err);
+  else
+    k_nearest<K, KIND, false><<<blocks, kQueryThreads, 0, s>>>(
+        t.tnodes, t.sorted, t.n, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, d_idx,
+        d_dist, bucket, err);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
+
+template <int KIND>
+abx_status nearest_dispatch(cudaStream_t s, TreeView const &t, const float *d_queries,
+                            int64_t nq, const uint32_t *d_perm, const int32_t *d_k, int32_t k,
+                            int32_t max_k, const int32_t *d_offsets, int32_t *d_offsets_out,
+                            int32_t *d_idx, float *d_dist)
+{
+  unsigned *err = device_state().d_error;
+#define ABX_KNN(KV)                                                                             \
+  return nearest_k<KV, KIND>(s, t, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, \
+                             d_idx, d_dist, err)
+  if (max_k <= 1)
+    ABX_KNN(1);
+  if (max_k <= 2)
+    ABX_KNN(2);
+  if (max_k <= 4)
+    ABX_KNN(4);
+  if (max_k <= 8)
+    ABX_KNN(8);
+  if (max_k <= 16)
+    ABX_KNN(16);
+  if (max_k <= 32)
+    ABX_KNN(32);
+#undef ABX_KNN
+  const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
+  const int bucket =
+      std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
+  k_nearest_large<KIND><<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.sorted, t.n, d_queries, nq,
+                                                         d_perm, d_k, k, d_offsets,
+                                                         d_offsets_out, d_idx, d_dist, bucket,
+                                                         err);
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
 }
@@ -560,12 +777,18 @@ abx_status launch_spatial(cudaStream_t s, TreeView const &t, abx_geometry pred_k
 {
   if (nq <= 0 || t.n <= 0)
     return ABX_SUCCESS;
+  StageScope scope(s, "spatial", 1);
+  const bool box_leaves = t.kind == ABX_BOX;
   if (pred_kind == ABX_SPHERE)
-    return spatial_dispatch<ABX_SPHERE>(s, t, d_preds, nq, d_perm, mode, d_counts, d_offsets,
-                                        d_out, buffer, d_overflow);
+    return box_leaves ? spatial_dispatch<ABX_SPHERE, 1>(s, t, d_preds, nq, d_perm, mode, d_counts,
+                                                        d_offsets, d_out, buffer, d_overflow)
+                      : spatial_dispatch<ABX_SPHERE, 0>(s, t, d_preds, nq, d_perm, mode, d_counts,
+                                                        d_offsets, d_out, buffer, d_overflow);
   if (pred_kind == ABX_BOX)
-    return spatial_dispatch<ABX_BOX>(s, t, d_preds, nq, d_perm, mode, d_counts, d_offsets,
-                                     d_out, buffer, d_overflow);
+    return box_leaves ? spatial_dispatch<ABX_BOX, 1>(s, t, d_preds, nq, d_perm, mode, d_counts,
+                                                     d_offsets, d_out, buffer, d_overflow)
+                      : spatial_dispatch<ABX_BOX, 0>(s, t, d_preds, nq, d_perm, mode, d_counts,
+                                                     d_offsets, d_out, buffer, d_overflow);
   return fail(ABX_ERROR_INVALID_ARGUMENT, "intersects predicates must be spheres or boxes");
 }
 
@@ -574,7 +797,7 @@ abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int3
 {
   if (nq <= 0)
     return ABX_SUCCESS;
-  unsigned blocks = (unsigned)((nq * 32 + 255) / 256);
+  const unsigned blocks = (unsigned)((nq * 32 + 255) / 256);
   StageScope scope(s, "compact", 1);
   k_compact<<<blocks, 256, 0, s>>>(d_tmp, nq, buffer, d_offsets, d_out);
   ABX_CUDA_TRY(cudaGetLastError());
@@ -588,32 +811,12 @@ abx_status launch_nearest(cudaStream_t s, TreeView const &t, const float *d_quer
 {
   if (nq <= 0)
     return ABX_SUCCESS;
-  unsigned *err = device_state().d_error;
-  unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
   StageScope scope(s, "nearest", 1);
-#define ABX_KNN(KV)                                                                        \
-  k_nearest<KV><<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.n, d_queries, nq, d_perm, d_k, \
-                                                 k, d_offsets, d_offsets_out, d_idx, d_dist, \
-                                                 err)
-  if (max_k <= 1)
-    ABX_KNN(1);
-  else if (max_k <= 2)
-    ABX_KNN(2);
-  else if (max_k <= 4)
-    ABX_KNN(4);
-  else if (max_k <= 8)
-    ABX_KNN(8);
-  else if (max_k <= 16)
-    ABX_KNN(16);
-  else if (max_k <= 32)
-    ABX_KNN(32);
-  else
-    k_nearest_large<<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.n, d_queries, nq, d_perm, d_k,
-                                                     k, d_offsets, d_offsets_out, d_idx,
-                                                     d_dist, err);
-#undef ABX_KNN
-  ABX_CUDA_TRY(cudaGetLastError());
-  return ABX_SUCCESS;
+  if (t.kind == ABX_BOX)
+    return nearest_dispatch<1>(s, t, d_queries, nq, d_perm, d_k, k, max_k, d_offsets,
+                               d_offsets_out, d_idx, d_dist);
+  return nearest_dispatch<0>(s, t, d_queries, nq, d_perm, d_k, k, max_k, d_offsets,
+                             d_offsets_out, d_idx, d_dist);
 }
 
 abx_status launch_knn_counts(cudaStream_t s, const int32_t *d_k, int64_t nq, int64_t n,
@@ -621,7 +824,7 @@ abx_status launch_knn_counts(cudaStream_t s, const int32_t *d_k, int64_t nq, int
 {
   if (nq <= 0)
     return ABX_SUCCESS;
-  unsigned blocks = (unsigned)((nq + 255) / 256);
+  const unsigned blocks = (unsigned)((nq + 255) / 256);
   StageScope scope(s, "knn_counts", 1);
   k_knn_counts<<<blocks, 256, 0, s>>>(d_k, nq, n, d_counts, d_max);
   ABX_CUDA_TRY(cudaGetLastError());

@@ -123,7 +123,7 @@ struct PassSmem
 // inclusive prefix; words of earlier passes read as "not ready", so one
 // buffer (zeroed once per sort) serves every pass.
 template <class K>
-__global__ void __launch_bounds__(kSortThreads)
+__global__ void __launch_bounds__(kSortThreads, 3)
     k_onesweep(const K *__restrict__ keys_in, const uint32_t *__restrict__ vals_in,
                K *__restrict__ keys_out, uint32_t *__restrict__ vals_out, int64_t n,
                int shift, int pass, const uint32_t *__restrict__ goffsets,
@@ -164,16 +164,14 @@ __global__ void __launch_bounds__(kSortThreads)
     }
   }
 
-  // 2. warp-level stable ranking
-  uint32_t rank[kItems];
-  unsigned dig[kItems];
+  // 2. warp-level stable ranking; dr[j] = digit << 16 | rank in the warp
+  uint32_t dr[kItems];
   const unsigned lt = lanemask_lt();
 #pragma unroll
   for (int j = 0; j < kItems; ++j)
   {
     int64_t idx = warp_base + j * 32;
     unsigned d = idx < n ? digit_of(key[j], shift) : (unsigned)kBins;
-    dig[j] = d;
     unsigned peers = __match_any_sync(0xffffffffu, d);
     int leader = __ffs(peers) - 1;
     uint32_t base = 0;
@@ -183,7 +181,7 @@ __global__ void __launch_bounds__(kSortThreads)
       sm.u.whist[warp][d] = base + __popc(peers);
     }
     base = __shfl_sync(0xffffffffu, base, leader);
-    rank[j] = base + __popc(peers & lt);
+    dr[j] = (d << 16) | (base + __popc(peers & lt));
     __syncwarp();
   }
   __syncthreads();
@@ -229,10 +227,12 @@ __global__ void __launch_bounds__(kSortThreads)
   }
   __syncthreads();
 
-  uint32_t pos[kItems];
 #pragma unroll
   for (int j = 0; j < kItems; ++j)
-    pos[j] = sm.digit_start[dig[j]] + sm.u.whist[warp][dig[j]] + rank[j];
+  {
+    const unsigned d = dr[j] >> 16;
+    dr[j] = sm.digit_start[d] + sm.u.whist[warp][d] + (dr[j] & 0xffffu); // tile position
+  }
 
   // 4. decoupled look-back, one digit per thread
   {
@@ -278,8 +278,8 @@ __global__ void __launch_bounds__(kSortThreads)
 #pragma unroll
   for (int j = 0; j < kItems; ++j)
   {
-    sm.u.exch.keys[pos[j]] = key[j];
-    sm.u.exch.vals[pos[j]] = val[j];
+    sm.u.exch.keys[dr[j]] = key[j];
+    sm.u.exch.vals[dr[j]] = val[j];
   }
   __syncthreads();
   const uint32_t valid = sm.digit_start[kBins];

@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1_000_000,
                     help="queries timed per CPU step (scaled to --nq)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--case", default="knn", choices=["knn", "build", "nearest", "radius"],
+                    help="knn: the benchmark step (build + kNN); build / nearest / radius: "
+                    "one stage alone (profiling cases; radius = 2-pass CRS search with "
+                    "~32 expected neighbours)")
     return ap.parse_args()
 
 
@@ -474,10 +478,69 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_case(args):
+    """One stage alone, W untimed + K timed repetitions, stage times from the
+    library's CUDA events (used for profiling captures of single kernels)."""
+    import ctypes
+
+    import torch
+
+    import arborx_gb300 as ax
+    from arborx_gb300 import _lib
+    from arborx_gb300 import build as libbuild
+
+    libbuild.build()
+    L = _lib.load()
+    points_np, queries_np = make_inputs(args.n, args.nq, 0)
+    points = torch.from_numpy(points_np).cuda()
+    queries = torch.from_numpy(queries_np).cuda()
+    r = float(np.float32((32 * 3 / (4 * np.pi * args.n)) ** (1 / 3)))
+    bvh = ax.BoundingVolumeHierarchy(points) if args.case != "build" else None
+
+    def once():
+        if args.case == "build":
+            return ax.BoundingVolumeHierarchy(points)
+        if args.case == "nearest":
+            return ax.query(bvh, ax.nearest(queries, args.k))
+        return ax.query(bvh, ax.make_intersects(queries, r))
+
+    for _ in range(args.warmup):
+        keep = once()
+    torch.cuda.synchronize()
+    L.abx_profiling_reset()
+    L.abx_profiling_enable(1)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        keep = once()
+    e1.record()
+    torch.cuda.synchronize()
+    L.abx_profiling_enable(0)
+    del keep
+    ms = e0.elapsed_time(e1) / args.steps
+    stages = {}
+    for name in ("bounds", "morton64", "sort64", "hierarchy", "morton32", "sort32", "nearest",
+                 "spatial", "scan"):
+        t = ctypes.c_double(0)
+        c = ctypes.c_int64(0)
+        L.abx_profiling_stage(name.encode(), ctypes.byref(t), ctypes.byref(c))
+        if c.value:
+            stages[name] = t.value / args.steps
+    units = args.n if args.case == "build" else args.nq
+    print(json.dumps({
+        "case": args.case, "n": args.n, "nq": args.nq, "k": args.k, "ms_per_step": ms,
+        "value": units / (ms * 1e-3), "unit": "points/s" if args.case == "build" else "queries/s",
+        "stages_ms": stages,
+    }), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.case != "knn":
+        run_case(args)
     else:
         run_gpu(args)
 

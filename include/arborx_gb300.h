@@ -108,6 +108,17 @@ ABX_API abx_status abx_profiling_stage(const char *stage, double *h_total_ms,
                                        int64_t *h_launches);
 ABX_API abx_status abx_profiling_reset(void);
 
+/* Launch-shape and kernel-variant knobs (no counterpart in the reference,
+ * whose launch shapes are Kokkos' RangePolicy defaults).  Known names:
+ * "SPATIAL_BUCKET" / "NEAREST_BUCKET" (a spatial / nearest traversal scans
+ * the leaves of any subtree of at most this many leaves from the
+ * Morton-ordered leaf copy instead of descending into it; 1-32, defaults 8
+ * and 1; read at query time).
+ * Unset knobs read the environment variable ABX_TUNE_<name>, then the
+ * built-in default.  Results never depend on a knob. */
+ABX_API abx_status abx_tuning_set(const char *name, int32_t value);
+ABX_API abx_status abx_tuning_reset(void);
+
 /* ---------------------------------------------------------------------- */
 /* Tree                                                                     */
 /* ---------------------------------------------------------------------- */

@@ -251,3 +251,36 @@ def test_exclusive_scan_and_crs_query_impl(ax, golden):
     big = np.random.default_rng(5).integers(0, 40, size=3_000_001).astype(np.int32)
     got = host(ax.exclusive_scan(cuda(big)))
     assert np.array_equal(got[:-1], o.exclusive_scan(big)) and got[-1] == big.sum()
+
+
+@pytest.mark.parametrize("bucket", [1, 2, 5, 8, 32])
+def test_results_do_not_depend_on_bucket_size(ax, bucket):
+    # the query-time bucket limits are tuning knobs: kNN and spatial results
+    # (order included) are the same for every value
+    L = ax._lib.load()
+    p = uniform_points(100000, 121)
+    q = uniform_points(20000, 122)
+    ref = o.OracleTree(p)
+    bvh = ax.BoundingVolumeHierarchy(cuda(p))
+    ax._lib.check(L.abx_tuning_set(b"SPATIAL_BUCKET", bucket))
+    ax._lib.check(L.abx_tuning_set(b"NEAREST_BUCKET", bucket))
+    try:
+        _check_variant_results(ax, bvh, ref, q)
+    finally:
+        L.abx_tuning_reset()
+
+
+def _check_variant_results(ax, bvh, ref, q):
+    for k in (1, 7, 16, 32, 40):
+        roff, rind, rdist = ref.nearest(q, k)
+        ind, off, dist = ax.query(bvh, ax.nearest(cuda(q), k), with_distances=True)
+        assert np.array_equal(host(ind), rind) and np.array_equal(host(dist), rdist)
+    spheres = _spheres(q, 0.02)
+    roff, rind = ref.spatial(o.KIND_SPHERE, spheres)
+    ind, off = ax.query(bvh, ax.intersects(cuda(spheres)))
+    assert np.array_equal(host(off), roff) and np.array_equal(host(ind), rind)
+    boxes = np.concatenate([q - 0.01, q + 0.01], axis=1).astype(np.float32)
+    roff, rind = ref.spatial(o.KIND_BOX, boxes)
+    ind, off = ax.query(bvh, ax.intersects(cuda(boxes)))
+    assert np.array_equal(host(off), roff) and np.array_equal(host(ind), rind)
+    assert ax.device_errors() == 0
