@@ -30,6 +30,11 @@ _I32 = ctypes.c_int32
 _STATUS = ctypes.c_int
 
 
+class DeviceViewC(ctypes.Structure):
+    _fields_ = [("nodes", ctypes.c_void_p), ("leaves", ctypes.c_void_p), ("size", ctypes.c_int64),
+                ("geometry", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class TraversalPolicyC(ctypes.Structure):
     _fields_ = [("buffer_size", ctypes.c_int32), ("sort_predicates", ctypes.c_int32)]
 
@@ -50,6 +55,7 @@ SIGNATURES = {
     "abx_bvh_bounds": (_STATUS, [_P, _P]),
     "abx_bvh_geometry": (ctypes.c_int, [_P]),
     "abx_bvh_export_nodes": (_STATUS, [_P, _P, _P, _P]),
+    "abx_bvh_device_view": (_STATUS, [_P, ctypes.POINTER(DeviceViewC)]),
     "abx_bvh_query_intersects": (
         _STATUS,
         [_P, _P, ctypes.c_int, _P, _I64, TraversalPolicyC, ctypes.POINTER(_P)],

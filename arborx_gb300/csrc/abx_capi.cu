@@ -473,6 +473,18 @@ abx_status abx_bvh_export_nodes(const abx_bvh *bvh, void *stream, int32_t *d_lea
   return ABX_SUCCESS;
 }
 
+abx_status abx_bvh_device_view(const abx_bvh *bvh, abx_device_view *out)
+{
+  if (!bvh || !out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_device_view: null argument");
+  out->nodes = bvh->tnodes;
+  out->leaves = bvh->sorted;
+  out->size = bvh->n;
+  out->geometry = bvh->kind;
+  out->reserved = 0;
+  return ABX_SUCCESS;
+}
+
 abx_status abx_bvh_query_intersects(const abx_bvh *bvh, void *stream, abx_geometry kind,
                                     const float *d_predicates, int64_t nq,
                                     abx_traversal_policy policy, abx_crs **out)

@@ -154,6 +154,31 @@ ABX_API abx_geometry abx_bvh_geometry(const abx_bvh *bvh);
 ABX_API abx_status abx_bvh_export_nodes(const abx_bvh *bvh, void *stream,
                                 int32_t *d_leaves, void *d_internal);
 
+/* Device view of a tree, for user kernels that traverse it themselves (the
+ * PerThread query, ArborX_LinearBVH.hpp:112-122; the callback query,
+ * :258-313).  `nodes` holds max(size - 1, 1) 64-byte child-pair nodes:
+ *   float4 a = L.lo.x L.lo.y L.lo.z L.hi.x
+ *   float4 b = L.hi.y L.hi.z R.lo.x R.lo.y
+ *   float4 c = R.lo.z R.hi.x R.hi.y R.hi.z
+ *   int4   d = left ref, right ref, left count, right count
+ * (root = node 0).  A ref >= 0 is an internal node.  A ref < 0 is a leaf with
+ * value ~ref whose bounding volume is the child box (count 1), or no child
+ * (count 0, one-leaf tree).  The count of an internal child is its number of
+ * leaves when at most 32 (bit 16 set: its index is the right end of its leaf
+ * range), else 0.  `leaves` holds the leaves in Morton order: points as
+ * float4 {x, y, z, value}, boxes as two float4 {lo, value} {hi, 0}.  Valid
+ * while the tree lives, once its build has completed on its stream. */
+typedef struct abx_device_view
+{
+  const void *nodes;
+  const void *leaves;
+  int64_t size;
+  int32_t geometry;
+  int32_t reserved;
+} abx_device_view;
+
+ABX_API abx_status abx_bvh_device_view(const abx_bvh *bvh, abx_device_view *out);
+
 /* ---------------------------------------------------------------------- */
 /* Queries with CRS output                                                  */
 /* ---------------------------------------------------------------------- */

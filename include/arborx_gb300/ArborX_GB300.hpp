@@ -1,0 +1,311 @@
+// ArborX_GB300.hpp -- C++ face of the GB300 BVH, shaped like ArborX's API.
+//
+// Header-only host code over the C ABI of arborx_gb300.h.  The names, the
+// argument meaning and the error behaviour follow the reference:
+//   BoundingVolumeHierarchy / BVH      src/spatial/ArborX_LinearBVH.hpp:57-142
+//   query(tree, space, preds, indices, offsets[, policy])
+//                                      src/spatial/ArborX_CrsGraphWrapper.hpp:22-34
+//   intersects / nearest               src/spatial/detail/ArborX_Predicates.hpp:57-142
+//   Experimental::make_intersects / make_nearest
+//                                      src/spatial/detail/ArborX_PredicateHelpers.hpp:92-206
+//   Experimental::TraversalPolicy      src/spatial/detail/ArborX_TraversalPolicy.hpp:19-47
+//   SearchException                    src/misc/ArborX_Exception.hpp:19-37
+// Device arrays play the role of Kokkos::View<T*, CudaSpace>; the execution
+// space instance is a cudaStream_t.  Values stored in the tree are the
+// indices of the input rows (the benchmark form BVH<MemorySpace, int, ...>).
+#ifndef ARBORX_GB300_HPP
+#define ARBORX_GB300_HPP
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <utility>
+#include <vector>
+
+#include "../arborx_gb300.h"
+
+namespace ArborXGB
+{
+
+// ArborX::SearchException (src/misc/ArborX_Exception.hpp:19-37).
+class SearchException : public std::logic_error
+{
+public:
+  explicit SearchException(std::string const &msg) : std::logic_error(msg) {}
+};
+
+namespace Details
+{
+inline void check(abx_status s)
+{
+  if (s == ABX_SUCCESS)
+    return;
+  std::string msg = std::string(abx_status_string(s)) + ": " + abx_last_error();
+  if (s == ABX_ERROR_BUFFER_OVERFLOW || s == ABX_ERROR_INVALID_ARGUMENT)
+    throw SearchException(msg);
+  throw std::runtime_error(msg);
+}
+inline void check_cuda(cudaError_t e)
+{
+  if (e != cudaSuccess)
+    throw std::runtime_error(std::string("CUDA: ") + cudaGetErrorString(e));
+}
+} // namespace Details
+
+// Geometries, memory-compatible with the ABI rows (and with ArborX::Point<3>,
+// ArborX::Box<3>, ArborX::Sphere<3> of float).
+struct Point
+{
+  float coords[3];
+  __host__ __device__ float &operator[](int d) { return coords[d]; }
+  __host__ __device__ float operator[](int d) const { return coords[d]; }
+};
+
+struct Box
+{
+  Point min_corner{{3.40282347e38f, 3.40282347e38f, 3.40282347e38f}};
+  Point max_corner{{-3.40282347e38f, -3.40282347e38f, -3.40282347e38f}};
+  Box() = default; // the empty box, ArborX_Box.hpp:35-42
+  __host__ __device__ Box(Point lo, Point hi) : min_corner(lo), max_corner(hi) {}
+  __host__ __device__ Point &minCorner() { return min_corner; }
+  __host__ __device__ Point const &minCorner() const { return min_corner; }
+  __host__ __device__ Point &maxCorner() { return max_corner; }
+  __host__ __device__ Point const &maxCorner() const { return max_corner; }
+};
+
+struct Sphere
+{
+  Point centre;
+  float r;
+  __host__ __device__ Point const &centroid() const { return centre; }
+  __host__ __device__ float radius() const { return r; }
+};
+
+static_assert(sizeof(Point) == 12 && sizeof(Box) == 24 && sizeof(Sphere) == 16,
+              "geometry rows must match the C ABI");
+
+// A device array owning its memory: the counterpart of
+// Kokkos::View<T*, Kokkos::CudaSpace>.
+template <class T>
+class DeviceView
+{
+public:
+  DeviceView() = default;
+  explicit DeviceView(size_t n) { realloc(n); }
+  DeviceView(std::vector<T> const &host, cudaStream_t s = nullptr)
+  {
+    realloc(host.size());
+    if (!host.empty())
+    {
+      Details::check_cuda(cudaMemcpyAsync(_ptr.get(), host.data(), host.size() * sizeof(T),
+                                          cudaMemcpyHostToDevice, s));
+      Details::check_cuda(cudaStreamSynchronize(s));
+    }
+  }
+  void realloc(size_t n)
+  {
+    _size = n;
+    T *p = nullptr;
+    if (n > 0)
+      Details::check_cuda(cudaMalloc(&p, n * sizeof(T)));
+    _ptr.reset(p, [](T *q) {
+      if (q)
+        cudaFree(q);
+    });
+  }
+  T *data() const { return _ptr.get(); }
+  size_t size() const { return _size; }
+  std::vector<T> to_host(cudaStream_t s = nullptr) const
+  {
+    std::vector<T> h(_size);
+    if (_size)
+    {
+      Details::check_cuda(
+          cudaMemcpyAsync(h.data(), _ptr.get(), _size * sizeof(T), cudaMemcpyDeviceToHost, s));
+      Details::check_cuda(cudaStreamSynchronize(s));
+    }
+    return h;
+  }
+
+private:
+  std::shared_ptr<T> _ptr;
+  size_t _size = 0;
+};
+
+namespace Experimental
+{
+// ArborX::Experimental::TraversalPolicy (ArborX_TraversalPolicy.hpp:19-47).
+struct TraversalPolicy
+{
+  int _buffer_size = 0;
+  bool _sort_predicates = true;
+  TraversalPolicy &setBufferSize(int buffer_size)
+  {
+    _buffer_size = buffer_size;
+    return *this;
+  }
+  TraversalPolicy &setPredicateSorting(bool sort_predicates)
+  {
+    _sort_predicates = sort_predicates;
+    return *this;
+  }
+};
+} // namespace Experimental
+
+// A batch of intersects(geometry) predicates over a device array.
+template <class Geometry>
+struct Intersects
+{
+  static_assert(std::is_same_v<Geometry, Sphere> || std::is_same_v<Geometry, Box>,
+                "intersects predicates are spheres or boxes");
+  DeviceView<Geometry> geometries;
+};
+
+// A batch of nearest(point, k) predicates (one k for all, or one per query).
+struct Nearest
+{
+  DeviceView<Point> points;
+  int k = 1;
+  DeviceView<int> ks; // empty = use k
+};
+
+template <class Geometry>
+Intersects<Geometry> intersects(DeviceView<Geometry> const &geometries)
+{
+  return Intersects<Geometry>{geometries};
+}
+
+inline Nearest nearest(DeviceView<Point> const &points, int k = 1) { return Nearest{points, k, {}}; }
+inline Nearest nearest(DeviceView<Point> const &points, DeviceView<int> const &ks)
+{
+  return Nearest{points, 0, ks};
+}
+
+namespace Experimental
+{
+// make_intersects(points, r) (ArborX_PredicateHelpers.hpp:99-105): spheres of
+// radius r around host points.
+inline Intersects<Sphere> make_intersects(std::vector<Point> const &points, float r,
+                                          cudaStream_t s = nullptr)
+{
+  std::vector<Sphere> spheres(points.size());
+  for (size_t i = 0; i < points.size(); ++i)
+    spheres[i] = Sphere{points[i], r};
+  return Intersects<Sphere>{DeviceView<Sphere>(spheres, s)};
+}
+inline Nearest make_nearest(DeviceView<Point> const &points, int k) { return nearest(points, k); }
+} // namespace Experimental
+
+class BoundingVolumeHierarchy
+{
+public:
+  using size_type = int64_t;
+  using bounding_volume_type = Box;
+  using value_type = int;
+
+  BoundingVolumeHierarchy() : BoundingVolumeHierarchy(nullptr, DeviceView<Point>()) {}
+
+  // BoundingVolumeHierarchy(space, values) (ArborX_LinearBVH.hpp:68-73)
+  BoundingVolumeHierarchy(cudaStream_t space, DeviceView<Point> const &points)
+  {
+    create(space, ABX_POINT, reinterpret_cast<const float *>(points.data()),
+           (int64_t)points.size());
+  }
+  BoundingVolumeHierarchy(cudaStream_t space, DeviceView<Box> const &boxes)
+  {
+    create(space, ABX_BOX, reinterpret_cast<const float *>(boxes.data()), (int64_t)boxes.size());
+  }
+
+  size_type size() const noexcept { return abx_bvh_size(_tree.get()); }
+  bool empty() const noexcept { return size() == 0; }
+  Box bounds() const
+  {
+    float b[6];
+    Details::check(abx_bvh_bounds(_tree.get(), b));
+    return Box(Point{{b[0], b[1], b[2]}}, Point{{b[3], b[4], b[5]}});
+  }
+
+  // query(space, predicates, indices, offsets[, policy]): the callee
+  // reallocates indices and offsets (ArborX_CrsGraphWrapperImpl.hpp:376-377).
+  template <class Geometry>
+  void query(cudaStream_t space, Intersects<Geometry> const &preds, DeviceView<int> &indices,
+             DeviceView<int> &offsets,
+             Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy()) const
+  {
+    abx_crs *crs = nullptr;
+    constexpr abx_geometry kind = std::is_same_v<Geometry, Sphere> ? ABX_SPHERE : ABX_BOX;
+    Details::check(abx_bvh_query_intersects(
+        _tree.get(), space, kind, reinterpret_cast<const float *>(preds.geometries.data()),
+        (int64_t)preds.geometries.size(), c_policy(policy), &crs));
+    take(space, crs, (int64_t)preds.geometries.size(), indices, offsets, nullptr);
+  }
+
+  void query(cudaStream_t space, Nearest const &preds, DeviceView<int> &indices,
+             DeviceView<int> &offsets,
+             Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy(),
+             DeviceView<float> *distances = nullptr) const
+  {
+    abx_crs *crs = nullptr;
+    Details::check(abx_bvh_query_nearest(
+        _tree.get(), space, reinterpret_cast<const float *>(preds.points.data()),
+        (int64_t)preds.points.size(), preds.ks.size() ? preds.ks.data() : nullptr, preds.k,
+        c_policy(policy), distances ? 1 : 0, &crs));
+    take(space, crs, (int64_t)preds.points.size(), indices, offsets, distances);
+  }
+
+  abx_bvh const *handle() const { return _tree.get(); }
+
+private:
+  void create(cudaStream_t space, abx_geometry kind, const float *values, int64_t n)
+  {
+    abx_bvh *t = nullptr;
+    Details::check(abx_bvh_create(space, kind, values, n, &t));
+    _tree.reset(t, [](abx_bvh *p) { abx_bvh_destroy(p); });
+  }
+  static abx_traversal_policy c_policy(Experimental::TraversalPolicy const &p)
+  {
+    return abx_traversal_policy{p._buffer_size, p._sort_predicates ? 1 : 0};
+  }
+  static void take(cudaStream_t space, abx_crs *crs, int64_t nq, DeviceView<int> &indices,
+                   DeviceView<int> &offsets, DeviceView<float> *distances)
+  {
+    std::unique_ptr<abx_crs, abx_status (*)(abx_crs *)> guard(crs, abx_crs_destroy);
+    const int64_t nres = abx_crs_num_results(crs);
+    offsets.realloc((size_t)nq + 1);
+    indices.realloc((size_t)nres);
+    Details::check_cuda(cudaMemcpyAsync(offsets.data(), abx_crs_offsets(crs),
+                                        (nq + 1) * sizeof(int), cudaMemcpyDeviceToDevice, space));
+    if (nres)
+      Details::check_cuda(cudaMemcpyAsync(indices.data(), abx_crs_indices(crs),
+                                          nres * sizeof(int), cudaMemcpyDeviceToDevice, space));
+    if (distances)
+    {
+      distances->realloc((size_t)nres);
+      if (nres)
+        Details::check_cuda(cudaMemcpyAsync(distances->data(), abx_crs_distances(crs),
+                                            nres * sizeof(float), cudaMemcpyDeviceToDevice,
+                                            space));
+    }
+  }
+
+  std::shared_ptr<abx_bvh> _tree;
+};
+
+using BVH = BoundingVolumeHierarchy;
+
+// ArborX::query(tree, space, predicates, indices, offsets[, policy])
+// (src/spatial/ArborX_CrsGraphWrapper.hpp:22-34).
+template <class Predicates>
+void query(BoundingVolumeHierarchy const &tree, cudaStream_t space, Predicates const &preds,
+           DeviceView<int> &indices, DeviceView<int> &offsets,
+           Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy())
+{
+  tree.query(space, preds, indices, offsets, policy);
+}
+
+} // namespace ArborXGB
+
+#endif // ARBORX_GB300_HPP
