@@ -64,6 +64,20 @@ SIGNATURES = {
         _STATUS,
         [_P, _P, _P, _I64, _P, _I32, TraversalPolicyC, _I32, ctypes.POINTER(_P)],
     ),
+    "abx_forest_create": (_STATUS, [_P, ctypes.c_int, _P, _P, _I32, ctypes.POINTER(_P)]),
+    "abx_forest_destroy": (_STATUS, [_P]),
+    "abx_forest_num_trees": (_I32, [_P]),
+    "abx_forest_size": (_I64, [_P, _I32]),
+    "abx_forest_bounds": (_STATUS, [_P, _I32, _P]),
+    "abx_forest_export_nodes": (_STATUS, [_P, _I32, _P, _P, _P]),
+    "abx_forest_query_intersects": (
+        _STATUS,
+        [_P, _P, ctypes.c_int, _P, _P, TraversalPolicyC, ctypes.POINTER(_P)],
+    ),
+    "abx_forest_query_nearest": (
+        _STATUS,
+        [_P, _P, _P, _P, _P, _I32, TraversalPolicyC, _I32, ctypes.POINTER(_P)],
+    ),
     "abx_crs_num_queries": (_I64, [_P]),
     "abx_crs_num_results": (_I64, [_P]),
     "abx_crs_offsets": (_P, [_P]),

@@ -12,6 +12,7 @@ plumbing); every computation is a kernel of libarborx_gb300.so.
 
 import ctypes
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -237,15 +238,111 @@ def query(tree, predicates, policy=None, space=None, with_distances=False):
         )
     else:
         raise TypeError("predicates must be Intersects or Nearest")
+    return _crs_result(h, isinstance(predicates, Nearest) and with_distances)
+
+
+def _crs_result(h, with_distances):
+    L = _lib.load()
     owner = _CrsOwner(h)
     nq = L.abx_crs_num_queries(h)
     nres = L.abx_crs_num_results(h)
     offsets = _view(owner, L.abx_crs_offsets(h), nq + 1, torch.int32)
     indices = _view(owner, L.abx_crs_indices(h), nres, torch.int32)
-    if isinstance(predicates, Nearest) and with_distances:
+    if with_distances:
         dist = _view(owner, L.abx_crs_distances(h), nres, torch.float32)
         return indices, offsets, dist
     return indices, offsets
+
+
+def _offsets_array(offsets, name):
+    o = np.ascontiguousarray(np.asarray(offsets, dtype=np.int64))
+    if o.ndim != 1 or o.size < 2:
+        raise ValueError("%s must hold at least two entries" % name)
+    return o
+
+
+class Forest:
+    """A batch of independent trees built together: tree t holds the rows
+    values[offsets[t]:offsets[t + 1]] and is exactly the tree that
+    BoundingVolumeHierarchy(values[offsets[t]:offsets[t + 1]]) builds (same
+    node arrays, tree-local values).  Replaces the reference's loop of one
+    BVH per subview (benchmarks/execution_space_instances/
+    execution_space_instances_driver.cpp:187-233)."""
+
+    def __init__(self, values, offsets, space=None, kind=None):
+        L = _lib.load()
+        self._h = ctypes.c_void_p()
+        if kind is None:
+            kind = {3: POINT, 6: BOX}.get(values.shape[-1])
+            if kind is None:
+                raise ValueError("values must have 3 (point) or 6 (box) columns")
+        self.kind = kind
+        v = _as_rows(values, 3 if kind == POINT else 6, "values")
+        o = _offsets_array(offsets, "offsets")
+        if o[-1] != v.shape[0]:
+            raise ValueError("offsets[-1] must equal the number of values")
+        self._offsets = o
+        self._stream = _stream(space)
+        check(L.abx_forest_create(self._stream, kind, _ptr(v), o.ctypes.data, o.size - 1,
+                                  ctypes.byref(self._h)))
+        self._values = v
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.load().abx_forest_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def num_trees(self):
+        return int(_lib.load().abx_forest_num_trees(self._h))
+
+    def size(self, tree):
+        return int(_lib.load().abx_forest_size(self._h, tree))
+
+    def bounds(self, tree):
+        out = (ctypes.c_float * 6)()
+        check(_lib.load().abx_forest_bounds(self._h, tree, out))
+        return tuple(out)
+
+    def export_nodes(self, tree, space=None):
+        """Node arrays of one tree, laid out like
+        BoundingVolumeHierarchy.export_nodes."""
+        n = self.size(tree)
+        leaves = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+        internal = torch.empty((max(n - 1, 0), 8), dtype=torch.int32, device="cuda")
+        check(_lib.load().abx_forest_export_nodes(self._h, tree, _stream(space), _ptr(leaves),
+                                                  _ptr(internal)))
+        return leaves, internal
+
+    def query(self, predicates, query_offsets, policy=None, space=None, with_distances=False):
+        """Predicates predicates[query_offsets[t]:query_offsets[t + 1]] run on
+        tree t.  Returns one CRS result over all queries with tree-local
+        indices: (indices, offsets[, distances])."""
+        L = _lib.load()
+        policy = policy or TraversalPolicy()
+        qo = _offsets_array(query_offsets, "query_offsets")
+        if qo.size != self._offsets.size:
+            raise ValueError("query_offsets needs one entry per tree plus one")
+        if qo[-1] != len(predicates):
+            raise ValueError("query_offsets[-1] must equal the number of predicates")
+        s = _stream(space)
+        h = ctypes.c_void_p()
+        if isinstance(predicates, Intersects):
+            check(L.abx_forest_query_intersects(self._h, s, predicates.kind, _ptr(predicates.data),
+                                                qo.ctypes.data, policy._c(), ctypes.byref(h)))
+            return _crs_result(h, False)
+        if isinstance(predicates, Nearest):
+            kt = predicates.k if isinstance(predicates.k, torch.Tensor) else None
+            kv = 0 if kt is not None else predicates.k
+            check(L.abx_forest_query_nearest(
+                self._h, s, _ptr(predicates.data), qo.ctypes.data,
+                _ptr(kt) if kt is not None else None, kv, policy._c(),
+                1 if with_distances else 0, ctypes.byref(h)))
+            return _crs_result(h, with_distances)
+        raise TypeError("predicates must be Intersects or Nearest")
 
 
 # ---------------------------------------------------------------------------

@@ -25,6 +25,29 @@ abx_status generate_hierarchy(cudaStream_t s, abx_geometry kind, const float *d_
                               LeafNode *d_leaves, InternalNode *d_internal, TNode *d_tnodes,
                               float4 *d_sorted);
 
+// Hierarchy over trees stored as segments [off[s], off[s+1]) of the sorted
+// positions (nseg trees; d_off on the device).  Node records of the
+// internal node with Karras index k of tree s go to slot off[s] + k; a
+// one-leaf tree has its traversal node in slot off[s].  Values and node
+// numbers in the records are tree-local.
+abx_status generate_hierarchy_segments(cudaStream_t s, abx_geometry kind, const float *d_g,
+                                       int64_t total, const int64_t *d_off, int nseg,
+                                       const uint32_t *d_perm, const uint64_t *d_codes,
+                                       LeafNode *d_leaves, InternalNode *d_internal,
+                                       TNode *d_tnodes, float4 *d_sorted);
+
+// Batched build of nseg trees given as segments of d_g (d_off on the device):
+// per-tree bounds (d_bounds, 6 floats per tree), per-tree Morton codes, a
+// stable sort of every tree, the segmented hierarchy.
+abx_status forest_build(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t total,
+                        const int64_t *d_off, int nseg, float *d_bounds, LeafNode *d_leaves,
+                        InternalNode *d_internal, TNode *d_tnodes, float4 *d_sorted);
+
+// Query order of a forest batch: by tree, then Morton32 within the tree's box.
+abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const float *d_preds,
+                              int64_t nq, const int64_t *d_qoff, int nseg,
+                              const float *d_bounds, uint32_t *d_perm);
+
 abx_status single_leaf(cudaStream_t s, abx_geometry kind, const float *d_g,
                        LeafNode *d_leaves, TNode *d_tnodes, float4 *d_sorted, float *d_bounds);
 
@@ -49,6 +72,16 @@ struct TreeView
   abx_geometry kind;     // ABX_POINT or ABX_BOX leaves
 };
 
+// Trees of a batch seen by a query launch: tree s owns the sorted positions
+// [tree_off[s], tree_off[s+1]) and the queries [qoff[s], qoff[s+1]).  A null
+// view means one tree (root node 0, TreeView::n leaves).
+struct ForestView
+{
+  const int64_t *tree_off;
+  const int64_t *qoff;
+  int nseg;
+};
+
 // Spatial query modes.
 enum SpatialMode
 {
@@ -57,23 +90,26 @@ enum SpatialMode
   kBuffered = 2 // out[q * buffer + j] for j < buffer, counts[q] = hits
 };
 
-abx_status launch_spatial(cudaStream_t s, TreeView const &t, abx_geometry pred_kind,
-                          const float *d_preds, int64_t nq, const uint32_t *d_perm,
-                          SpatialMode mode, int32_t *d_counts, const int32_t *d_offsets,
-                          int32_t *d_out, int32_t buffer, unsigned *d_overflow);
+abx_status launch_spatial(cudaStream_t s, TreeView const &t, ForestView const *f,
+                          abx_geometry pred_kind, const float *d_preds, int64_t nq,
+                          const uint32_t *d_perm, SpatialMode mode, int32_t *d_counts,
+                          const int32_t *d_offsets, int32_t *d_out, int32_t buffer,
+                          unsigned *d_overflow);
 
 abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int32_t buffer,
                           const int32_t *d_offsets, int32_t *d_out);
 
 // kNN: d_offsets null means uniform k (offset q * min(k, n)), and then
 // d_offsets_out (nq + 1) is filled by the kernel.  max_k bounds every k.
-abx_status launch_nearest(cudaStream_t s, TreeView const &t, const float *d_queries,
-                          int64_t nq, const uint32_t *d_perm, const int32_t *d_k,
-                          int32_t k, int32_t max_k, const int32_t *d_offsets,
+abx_status launch_nearest(cudaStream_t s, TreeView const &t, ForestView const *f,
+                          const float *d_queries, int64_t nq, const uint32_t *d_perm,
+                          const int32_t *d_k, int32_t k, int32_t max_k, const int32_t *d_offsets,
                           int32_t *d_offsets_out, int32_t *d_idx, float *d_dist);
 
-// counts[q] = min(max(k_q, 0), n), max over queries into *d_max (zeroed).
-abx_status launch_knn_counts(cudaStream_t s, const int32_t *d_k, int64_t nq, int64_t n,
-                             int32_t *d_counts, int32_t *d_max);
+// counts[q] = min(max(k_q, 0), size of q's tree) with k_q = d_k[q] (or k
+// when d_k is null); max of k_q over queries into *d_max (zeroed).
+abx_status launch_knn_counts(cudaStream_t s, TreeView const &t, ForestView const *f,
+                             const int32_t *d_k, int32_t k, int64_t nq, int32_t *d_counts,
+                             int32_t *d_max);
 
 } // namespace abx

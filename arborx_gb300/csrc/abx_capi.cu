@@ -27,9 +27,18 @@ struct abx_bvh
   abx::InternalNode *internal = nullptr;
   abx::TNode *tnodes = nullptr;
   float4 *sorted = nullptr;  // leaf geometry in Morton order (bucket scans)
-  float *d_bounds = nullptr; // tree bounds on the device (6 floats)
+  float *d_bounds = nullptr; // tree bounds on the device (6 floats per tree)
   float *h_bounds = nullptr; // pinned copy, valid once `ready` completed
   cudaEvent_t ready = nullptr;
+  // a batch of trees (abx_forest): tree s owns the sorted positions
+  // [h_off[s], h_off[s + 1]); empty for a single tree
+  int32_t ntrees = 1;
+  std::vector<int64_t> h_off;
+  int64_t *d_off = nullptr;
+};
+
+struct abx_forest : abx_bvh
+{
 };
 
 struct abx_crs
@@ -206,6 +215,7 @@ void destroy_tree(abx_bvh *t)
   dfree(t->tnodes, s);
   dfree(t->sorted, s);
   dfree(t->d_bounds, s);
+  dfree(t->d_off, s);
   if (t->h_bounds)
   {
     if (t->ready)
@@ -273,13 +283,46 @@ abx_status build_tree(abx_bvh *t, const float *d_values)
   return ABX_SUCCESS;
 }
 
-abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
-                           const float *d_preds, int64_t nq, Scratch<uint32_t> &perm)
+// Batched build: every tree of the forest in one pipeline (per-tree scene
+// boxes and Morton codes, one sort over all trees regrouped stably by tree,
+// one hierarchy pass over all segments).
+abx_status build_forest(abx_bvh *t, const float *d_values)
 {
+  cudaStream_t s = t->stream;
+  const int nt = t->ntrees;
+  const int64_t total = t->n;
+  ABX_CUDA_TRY(dmalloc_n(&t->d_bounds, (size_t)6 * nt, s));
+  ABX_CUDA_TRY(dmalloc_n(&t->d_off, (size_t)nt + 1, s));
+  ABX_CUDA_TRY(cudaMemcpyAsync(t->d_off, t->h_off.data(), ((size_t)nt + 1) * sizeof(int64_t),
+                               cudaMemcpyHostToDevice, s));
+  if (total > 0)
+  {
+    const int f4 = t->kind == ABX_BOX ? 2 : 1;
+    ABX_CUDA_TRY(dmalloc_n(&t->leaves, total, s));
+    ABX_CUDA_TRY(dmalloc_n(&t->internal, total, s));
+    ABX_CUDA_TRY(dmalloc_n(&t->tnodes, total, s));
+    ABX_CUDA_TRY(dmalloc_n(&t->sorted, (size_t)total * f4, s));
+  }
+  ABX_TRY(forest_build(s, t->kind, d_values, total, t->d_off, nt, t->d_bounds, t->leaves,
+                       t->internal, t->tnodes, t->sorted));
+  ABX_CUDA_TRY(cudaMemcpyAsync(t->h_bounds, t->d_bounds, (size_t)6 * nt * sizeof(float),
+                               cudaMemcpyDeviceToHost, s));
+  return ABX_SUCCESS;
+}
+
+// Query order: Morton32 codes of the predicates in the scene box; in a
+// forest the tree index ranks above the code, the code taken in the tree's
+// own box.
+abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
+                           const float *d_preds, int64_t nq, const int64_t *qoff,
+                           Scratch<uint32_t> &perm)
+{
+  ABX_CUDA_TRY(perm.alloc(nq, s));
+  if (t->d_off)
+    return forest_query_order(s, kind, d_preds, nq, qoff, t->ntrees, t->d_bounds, perm.ptr);
   Scratch<uint32_t> codes;
   Scratch<uint32_t> hist;
   ABX_CUDA_TRY(codes.alloc(nq, s));
-  ABX_CUDA_TRY(perm.alloc(nq, s));
   ABX_CUDA_TRY(hist.alloc(4 * 256, s));
   ABX_CUDA_TRY(cudaMemsetAsync(hist.ptr, 0, 4 * 256 * sizeof(uint32_t), s));
   ABX_TRY(morton32_codes(s, kind, d_preds, nq, t->d_bounds, codes.ptr, hist.ptr));
@@ -290,6 +333,238 @@ abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
 TreeView view_of(const abx_bvh *t)
 {
   return TreeView{t->tnodes, t->n, t->d_bounds, t->sorted, t->kind};
+}
+
+// Check a forest's query offsets (0 first, non-decreasing, one entry per
+// tree plus one) and copy them to the device.
+abx_status upload_query_offsets(cudaStream_t s, const abx_bvh *t, const int64_t *h_qoff,
+                                Scratch<int64_t> &qoff, ForestView &fv)
+{
+  const int nt = t->ntrees;
+  ABX_CUDA_TRY(qoff.alloc((size_t)nt + 1, s));
+  ABX_CUDA_TRY(cudaMemcpyAsync(qoff.ptr, h_qoff, ((size_t)nt + 1) * sizeof(int64_t),
+                               cudaMemcpyHostToDevice, s));
+  // the source is the caller's host array: finish the copy before returning
+  ABX_CUDA_TRY(cudaStreamSynchronize(s));
+  fv = ForestView{t->d_off, qoff.ptr, nt};
+  return ABX_SUCCESS;
+}
+
+// Spatial query driver of a tree or a forest (h_qoff: the forest's query
+// offsets on the host, null for a tree).  Count, scan, fill
+// (ArborX_CrsGraphWrapperImpl.hpp:240-313), or one buffered pass with the
+// two-pass form as its overflow path (ArborX_CrsGraphWrapperImpl.hpp:117-238).
+abx_status query_intersects(const abx_bvh *bvh, cudaStream_t s, abx_geometry kind,
+                            const float *d_predicates, int64_t nq, const int64_t *h_qoff,
+                            abx_traversal_policy policy, abx_crs **out)
+{
+  device_state();
+  ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+
+  abx_crs *c = new (std::nothrow) abx_crs;
+  if (!c)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
+  cudaGetDevice(&c->device);
+  c->stream = s;
+  c->nq = nq;
+  auto bail = [&](abx_status st) {
+    cudaStreamSynchronize(s);
+    destroy_crs(c);
+    return st;
+  };
+  if (dmalloc_n(&c->offsets, nq + 1, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS offsets"));
+  if (bvh->n == 0 || nq == 0)
+  {
+    cudaMemsetAsync(c->offsets, 0, (nq + 1) * sizeof(int32_t), s);
+    dmalloc_n(&c->indices, 0, s);
+    *out = c;
+    return ABX_SUCCESS;
+  }
+  Scratch<int64_t> qoff;
+  ForestView fv{nullptr, nullptr, 1};
+  if (h_qoff)
+  {
+    abx_status st = upload_query_offsets(s, bvh, h_qoff, qoff, fv);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  const ForestView *f = h_qoff ? &fv : nullptr;
+  Scratch<uint32_t> perm;
+  if (policy.sort_predicates && nq > 1)
+  {
+    abx_status st = sort_predicates(s, bvh, kind, d_predicates, nq, qoff.ptr, perm);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  const TreeView tv = view_of(bvh);
+  const int64_t buffer = policy.buffer_size < 0 ? -(int64_t)policy.buffer_size
+                                                : (int64_t)policy.buffer_size;
+  int32_t total = 0;
+  if (buffer == 0)
+  {
+    abx_status st = launch_spatial(s, tv, f, kind, d_predicates, nq, perm.ptr, kCount, c->offsets,
+                                   nullptr, nullptr, 0, nullptr);
+    if (st == ABX_SUCCESS)
+      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    cudaMemcpyAsync(&total, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    st = sync_and_check(s);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
+    st = launch_spatial(s, tv, f, kind, d_predicates, nq, perm.ptr, kFill, nullptr, c->offsets,
+                        c->indices, 0, nullptr);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  else
+  {
+    if (buffer * nq > ((int64_t)1 << 33))
+      return bail(fail(ABX_ERROR_INVALID_ARGUMENT, "buffer_size x queries too large"));
+    Scratch<int32_t> tmp;
+    Scratch<unsigned> flag;
+    if (tmp.alloc((size_t)(buffer * nq), s) != cudaSuccess || flag.alloc(1, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS buffer"));
+    cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), s);
+    abx_status st = launch_spatial(s, tv, f, kind, d_predicates, nq, perm.ptr, kBuffered,
+                                   c->offsets, nullptr, tmp.ptr, (int32_t)buffer, flag.ptr);
+    if (st == ABX_SUCCESS)
+      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    unsigned overflow = 0;
+    cudaMemcpyAsync(&total, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&overflow, flag.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    st = sync_and_check(s);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    if (overflow && policy.buffer_size < 0)
+      return bail(fail(ABX_ERROR_BUFFER_OVERFLOW,
+                       "buffer_size " + std::to_string(policy.buffer_size) +
+                           " is too small for the results of some query"));
+    if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
+    if (!overflow)
+      st = launch_compact(s, tmp.ptr, nq, (int32_t)buffer, c->offsets, c->indices);
+    else
+      st = launch_spatial(s, tv, f, kind, d_predicates, nq, perm.ptr, kFill, nullptr, c->offsets,
+                          c->indices, 0, nullptr);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  c->nres = total;
+  *out = c;
+  return ABX_SUCCESS;
+}
+
+// Nearest query driver of a tree or a forest: offsets from the per-query
+// counts min(k, size of the query's tree) when k varies or trees differ,
+// else the fixed stride min(k, n); one traversal fills the CRS arrays.
+abx_status query_nearest(const abx_bvh *bvh, cudaStream_t s, const float *d_queries, int64_t nq,
+                         const int64_t *h_qoff, const int32_t *d_k, int32_t k,
+                         abx_traversal_policy policy, int32_t with_distances, abx_crs **out)
+{
+  device_state();
+  ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+
+  abx_crs *c = new (std::nothrow) abx_crs;
+  if (!c)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
+  cudaGetDevice(&c->device);
+  c->stream = s;
+  c->nq = nq;
+  auto bail = [&](abx_status st) {
+    cudaStreamSynchronize(s);
+    destroy_crs(c);
+    return st;
+  };
+  if (dmalloc_n(&c->offsets, nq + 1, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS offsets"));
+  const int64_t n = bvh->n;
+  if (n == 0 || nq == 0)
+  {
+    cudaMemsetAsync(c->offsets, 0, (nq + 1) * sizeof(int32_t), s);
+    dmalloc_n(&c->indices, 0, s);
+    if (with_distances)
+      dmalloc_n(&c->distances, 0, s);
+    *out = c;
+    return ABX_SUCCESS;
+  }
+  Scratch<int64_t> qoff;
+  ForestView fv{nullptr, nullptr, 1};
+  if (h_qoff)
+  {
+    abx_status st = upload_query_offsets(s, bvh, h_qoff, qoff, fv);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  const ForestView *f = h_qoff ? &fv : nullptr;
+  Scratch<uint32_t> perm;
+  if (policy.sort_predicates && nq > 1)
+  {
+    abx_status st = sort_predicates(s, bvh, ABX_POINT, d_queries, nq, qoff.ptr, perm);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+  }
+  const TreeView tv = view_of(bvh);
+  int64_t total = 0;
+  int32_t max_k = k;
+  const bool counted = d_k || f;
+  if (!counted)
+  {
+    if (k < 0)
+      k = 0;
+    const int64_t kk = std::min<int64_t>(k, n);
+    total = kk * nq;
+    if (total >= (int64_t)INT32_MAX)
+      return bail(fail(ABX_ERROR_INVALID_ARGUMENT, "nearest: more than 2^31-1 results"));
+  }
+  else
+  {
+    Scratch<int32_t> kmax;
+    if (kmax.alloc(1, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "scratch"));
+    cudaMemsetAsync(kmax.ptr, 0, sizeof(int32_t), s);
+    abx_status st = launch_knn_counts(s, tv, f, d_k, k, nq, c->offsets, kmax.ptr);
+    if (st == ABX_SUCCESS)
+      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    int32_t t32 = 0;
+    cudaMemcpyAsync(&t32, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&max_k, kmax.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+    st = sync_and_check(s);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    total = t32;
+  }
+  if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
+  Scratch<float> dist_tmp;
+  float *dist = nullptr;
+  if (with_distances)
+  {
+    if (dmalloc_n(&c->distances, (size_t)total, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS distances"));
+    dist = c->distances;
+  }
+  else if (max_k > 32)
+  {
+    if (dist_tmp.alloc((size_t)total, s) != cudaSuccess)
+      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "kNN heap"));
+    dist = dist_tmp.ptr;
+  }
+  abx_status st = launch_nearest(s, tv, f, d_queries, nq, perm.ptr, d_k, k, max_k,
+                                 counted ? c->offsets : nullptr, counted ? nullptr : c->offsets,
+                                 c->indices, dist);
+  if (st != ABX_SUCCESS)
+    return bail(st);
+  c->nres = total;
+  *out = c;
+  return ABX_SUCCESS;
 }
 
 } // namespace
@@ -492,6 +767,8 @@ abx_status abx_bvh_query_intersects(const abx_bvh *bvh, void *stream, abx_geomet
   if (!bvh || !out)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: null argument");
   *out = nullptr;
+  if (bvh->d_off)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: a forest handle");
   if (kind != ABX_SPHERE && kind != ABX_BOX)
     return fail(ABX_ERROR_INVALID_ARGUMENT,
                 "abx_bvh_query_intersects: predicates must be spheres or boxes");
@@ -499,98 +776,7 @@ abx_status abx_bvh_query_intersects(const abx_bvh *bvh, void *stream, abx_geomet
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: bad number of queries");
   if (nq > 0 && !d_predicates)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: null predicates");
-  cudaStream_t s = as_stream(stream);
-  device_state();
-  ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
-
-  abx_crs *c = new (std::nothrow) abx_crs;
-  if (!c)
-    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
-  cudaGetDevice(&c->device);
-  c->stream = s;
-  c->nq = nq;
-  auto bail = [&](abx_status st) {
-    cudaStreamSynchronize(s);
-    destroy_crs(c);
-    return st;
-  };
-  if (dmalloc_n(&c->offsets, nq + 1, s) != cudaSuccess)
-    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS offsets"));
-  if (bvh->n == 0 || nq == 0)
-  {
-    cudaMemsetAsync(c->offsets, 0, (nq + 1) * sizeof(int32_t), s);
-    dmalloc_n(&c->indices, 0, s);
-    *out = c;
-    return ABX_SUCCESS;
-  }
-  Scratch<uint32_t> perm;
-  if (policy.sort_predicates && nq > 1)
-  {
-    abx_status st = sort_predicates(s, bvh, kind, d_predicates, nq, perm);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-  }
-  const TreeView tv = view_of(bvh);
-  const int64_t buffer = policy.buffer_size < 0 ? -(int64_t)policy.buffer_size
-                                                : (int64_t)policy.buffer_size;
-  int32_t total = 0;
-  if (buffer == 0)
-  {
-    abx_status st = launch_spatial(s, tv, kind, d_predicates, nq, perm.ptr, kCount, c->offsets,
-                                   nullptr, nullptr, 0, nullptr);
-    if (st == ABX_SUCCESS)
-      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-    cudaMemcpyAsync(&total, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-    st = sync_and_check(s);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-    if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
-      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
-    st = launch_spatial(s, tv, kind, d_predicates, nq, perm.ptr, kFill, nullptr, c->offsets,
-                        c->indices, 0, nullptr);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-  }
-  else
-  {
-    if (buffer * nq > ((int64_t)1 << 33))
-      return bail(fail(ABX_ERROR_INVALID_ARGUMENT, "buffer_size x queries too large"));
-    Scratch<int32_t> tmp;
-    Scratch<unsigned> flag;
-    if (tmp.alloc((size_t)(buffer * nq), s) != cudaSuccess || flag.alloc(1, s) != cudaSuccess)
-      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS buffer"));
-    cudaMemsetAsync(flag.ptr, 0, sizeof(unsigned), s);
-    abx_status st = launch_spatial(s, tv, kind, d_predicates, nq, perm.ptr, kBuffered,
-                                   c->offsets, nullptr, tmp.ptr, (int32_t)buffer, flag.ptr);
-    if (st == ABX_SUCCESS)
-      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-    unsigned overflow = 0;
-    cudaMemcpyAsync(&total, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&overflow, flag.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
-    st = sync_and_check(s);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-    if (overflow && policy.buffer_size < 0)
-      return bail(fail(ABX_ERROR_BUFFER_OVERFLOW,
-                       "buffer_size " + std::to_string(policy.buffer_size) +
-                           " is too small for the results of some query"));
-    if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
-      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
-    if (!overflow)
-      st = launch_compact(s, tmp.ptr, nq, (int32_t)buffer, c->offsets, c->indices);
-    else
-      st = launch_spatial(s, tv, kind, d_predicates, nq, perm.ptr, kFill, nullptr, c->offsets,
-                          c->indices, 0, nullptr);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-  }
-  c->nres = total;
-  *out = c;
-  return ABX_SUCCESS;
+  return query_intersects(bvh, as_stream(stream), kind, d_predicates, nq, nullptr, policy, out);
 }
 
 abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream, const float *d_queries,
@@ -601,99 +787,170 @@ abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream, const float *
   if (!bvh || !out)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: null argument");
   *out = nullptr;
+  if (bvh->d_off)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: a forest handle");
   if (nq < 0 || nq >= (int64_t)INT32_MAX)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: bad number of queries");
   if (nq > 0 && !d_queries)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: null queries");
-  cudaStream_t s = as_stream(stream);
-  device_state();
-  ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+  return query_nearest(bvh, as_stream(stream), d_queries, nq, nullptr, d_k, k, policy,
+                       with_distances, out);
+}
 
-  abx_crs *c = new (std::nothrow) abx_crs;
-  if (!c)
-    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
-  cudaGetDevice(&c->device);
-  c->stream = s;
-  c->nq = nq;
-  auto bail = [&](abx_status st) {
-    cudaStreamSynchronize(s);
-    destroy_crs(c);
-    return st;
-  };
-  if (dmalloc_n(&c->offsets, nq + 1, s) != cudaSuccess)
-    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS offsets"));
-  const int64_t n = bvh->n;
-  if (n == 0 || nq == 0)
+abx_status abx_forest_create(void *stream, abx_geometry kind, const float *d_values,
+                             const int64_t *h_offsets, int32_t ntrees, abx_forest **out)
+{
+  if (!out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_create: null output handle");
+  *out = nullptr;
+  if (kind != ABX_POINT && kind != ABX_BOX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_create: values must be points or boxes");
+  if (ntrees < 1 || !h_offsets)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_create: need at least one tree");
+  if (h_offsets[0] != 0)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_create: offsets[0] must be 0");
+  for (int32_t i = 0; i < ntrees; ++i)
+    if (h_offsets[i + 1] < h_offsets[i])
+      return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_create: offsets must not decrease");
+  const int64_t total = h_offsets[ntrees];
+  if (total >= (int64_t)INT32_MAX / 2)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_create: more than 2^30-1 values");
+  if (total > 0 && !d_values)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_create: null values");
+  device_state();
+  abx_forest *t = new (std::nothrow) abx_forest;
+  if (!t)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_forest_create: host allocation");
+  cudaGetDevice(&t->device);
+  t->stream = as_stream(stream);
+  t->kind = kind;
+  t->n = total;
+  t->ntrees = ntrees;
+  t->h_off.assign(h_offsets, h_offsets + ntrees + 1);
+  cudaError_t e = cudaMallocHost(&t->h_bounds, (size_t)6 * ntrees * sizeof(float));
+  if (e != cudaSuccess)
   {
-    cudaMemsetAsync(c->offsets, 0, (nq + 1) * sizeof(int32_t), s);
-    dmalloc_n(&c->indices, 0, s);
-    if (with_distances)
-      dmalloc_n(&c->distances, 0, s);
-    *out = c;
-    return ABX_SUCCESS;
+    t->h_bounds = nullptr;
+    destroy_tree(t);
+    return fail_cuda(e, "cudaMallocHost");
   }
-  Scratch<uint32_t> perm;
-  if (policy.sort_predicates && nq > 1)
+  e = cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming);
+  if (e != cudaSuccess)
   {
-    abx_status st = sort_predicates(s, bvh, ABX_POINT, d_queries, nq, perm);
-    if (st != ABX_SUCCESS)
-      return bail(st);
+    t->ready = nullptr;
+    destroy_tree(t);
+    return fail_cuda(e, "cudaEventCreate");
   }
-  const TreeView tv = view_of(bvh);
-  int64_t total = 0;
-  int32_t max_k = k;
-  if (!d_k)
+  abx_status st = build_forest(t, d_values);
+  if (st == ABX_SUCCESS)
   {
-    if (k < 0)
-      k = 0;
-    const int64_t kk = std::min<int64_t>(k, n);
-    total = kk * nq;
-    if (total >= (int64_t)INT32_MAX)
-      return bail(fail(ABX_ERROR_INVALID_ARGUMENT, "nearest: more than 2^31-1 results"));
+    e = cudaEventRecord(t->ready, t->stream);
+    if (e != cudaSuccess)
+      st = fail_cuda(e, "cudaEventRecord");
   }
-  else
-  {
-    Scratch<int32_t> kmax;
-    if (kmax.alloc(1, s) != cudaSuccess)
-      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "scratch"));
-    cudaMemsetAsync(kmax.ptr, 0, sizeof(int32_t), s);
-    abx_status st = launch_knn_counts(s, d_k, nq, n, c->offsets, kmax.ptr);
-    if (st == ABX_SUCCESS)
-      st = exclusive_scan_i32(s, c->offsets, nq, c->offsets);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-    int32_t t32 = 0;
-    cudaMemcpyAsync(&t32, c->offsets + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&max_k, kmax.ptr, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
-    st = sync_and_check(s);
-    if (st != ABX_SUCCESS)
-      return bail(st);
-    total = t32;
-  }
-  if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
-    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
-  Scratch<float> dist_tmp;
-  float *dist = nullptr;
-  if (with_distances)
-  {
-    if (dmalloc_n(&c->distances, (size_t)total, s) != cudaSuccess)
-      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS distances"));
-    dist = c->distances;
-  }
-  else if (max_k > 32)
-  {
-    if (dist_tmp.alloc((size_t)total, s) != cudaSuccess)
-      return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "kNN heap"));
-    dist = dist_tmp.ptr;
-  }
-  abx_status st = launch_nearest(s, tv, d_queries, nq, perm.ptr, d_k, k, max_k,
-                                 d_k ? c->offsets : nullptr, d_k ? nullptr : c->offsets,
-                                 c->indices, dist);
   if (st != ABX_SUCCESS)
-    return bail(st);
-  c->nres = total;
-  *out = c;
+  {
+    cudaStreamSynchronize(t->stream);
+    destroy_tree(t);
+    return st;
+  }
+  *out = t;
   return ABX_SUCCESS;
+}
+
+abx_status abx_forest_destroy(abx_forest *forest)
+{
+  destroy_tree(forest);
+  return ABX_SUCCESS;
+}
+
+int32_t abx_forest_num_trees(const abx_forest *forest) { return forest ? forest->ntrees : 0; }
+
+int64_t abx_forest_size(const abx_forest *forest, int32_t tree)
+{
+  if (!forest || tree < 0 || tree >= forest->ntrees)
+    return 0;
+  return forest->h_off[tree + 1] - forest->h_off[tree];
+}
+
+abx_status abx_forest_bounds(const abx_forest *forest, int32_t tree, float h_box[6])
+{
+  if (!forest || !h_box || tree < 0 || tree >= forest->ntrees)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_bounds: bad argument");
+  ABX_CUDA_TRY(cudaEventSynchronize(forest->ready));
+  std::memcpy(h_box, forest->h_bounds + 6 * (size_t)tree, 6 * sizeof(float));
+  return ABX_SUCCESS;
+}
+
+abx_status abx_forest_export_nodes(const abx_forest *forest, int32_t tree, void *stream,
+                                   int32_t *d_leaves, void *d_internal)
+{
+  if (!forest || tree < 0 || tree >= forest->ntrees)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_export_nodes: bad argument");
+  cudaStream_t s = as_stream(stream);
+  ABX_CUDA_TRY(cudaStreamWaitEvent(s, forest->ready, 0));
+  const int64_t lo = forest->h_off[tree];
+  const int64_t n = forest->h_off[tree + 1] - lo;
+  if (d_leaves && n > 0)
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_leaves, forest->leaves + lo, n * sizeof(LeafNode),
+                                 cudaMemcpyDeviceToDevice, s));
+  if (d_internal && n > 1)
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_internal, forest->internal + lo,
+                                 (n - 1) * sizeof(InternalNode), cudaMemcpyDeviceToDevice, s));
+  return ABX_SUCCESS;
+}
+
+namespace
+{
+abx_status check_query_offsets(const abx_forest *forest, const int64_t *h_qoff, const char *who)
+{
+  if (!h_qoff)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, std::string(who) + ": null query offsets");
+  if (h_qoff[0] != 0)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, std::string(who) + ": query offsets[0] must be 0");
+  for (int32_t i = 0; i < forest->ntrees; ++i)
+    if (h_qoff[i + 1] < h_qoff[i])
+      return fail(ABX_ERROR_INVALID_ARGUMENT,
+                  std::string(who) + ": query offsets must not decrease");
+  if (h_qoff[forest->ntrees] >= (int64_t)INT32_MAX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, std::string(who) + ": bad number of queries");
+  return ABX_SUCCESS;
+}
+} // namespace
+
+abx_status abx_forest_query_intersects(const abx_forest *forest, void *stream,
+                                       abx_geometry kind, const float *d_predicates,
+                                       const int64_t *h_query_offsets,
+                                       abx_traversal_policy policy, abx_crs **out)
+{
+  if (!forest || !out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_query_intersects: null argument");
+  *out = nullptr;
+  if (kind != ABX_SPHERE && kind != ABX_BOX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT,
+                "abx_forest_query_intersects: predicates must be spheres or boxes");
+  ABX_TRY(check_query_offsets(forest, h_query_offsets, "abx_forest_query_intersects"));
+  const int64_t nq = h_query_offsets[forest->ntrees];
+  if (nq > 0 && !d_predicates)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_query_intersects: null predicates");
+  return query_intersects(forest, as_stream(stream), kind, d_predicates, nq, h_query_offsets,
+                          policy, out);
+}
+
+abx_status abx_forest_query_nearest(const abx_forest *forest, void *stream,
+                                    const float *d_queries, const int64_t *h_query_offsets,
+                                    const int32_t *d_k, int32_t k, abx_traversal_policy policy,
+                                    int32_t with_distances, abx_crs **out)
+{
+  if (!forest || !out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_query_nearest: null argument");
+  *out = nullptr;
+  ABX_TRY(check_query_offsets(forest, h_query_offsets, "abx_forest_query_nearest"));
+  const int64_t nq = h_query_offsets[forest->ntrees];
+  if (nq > 0 && !d_queries)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_query_nearest: null queries");
+  return query_nearest(forest, as_stream(stream), d_queries, nq, h_query_offsets, d_k, k, policy,
+                       with_distances, out);
 }
 
 int64_t abx_crs_num_queries(const abx_crs *crs) { return crs ? crs->nq : 0; }

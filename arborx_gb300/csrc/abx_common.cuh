@@ -376,6 +376,23 @@ struct SortedLeaf<1>
   }
 };
 
+// Segment containing global position i of a batch of trees: the largest s
+// with off[s] <= i (empty trees share offsets with their successor and are
+// skipped).
+__device__ __forceinline__ int find_segment(const int64_t *__restrict__ off, int nseg, int64_t i)
+{
+  int lo = 0, hi = nseg - 1;
+  while (lo < hi)
+  {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(off + mid) <= i)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 // ---------------------------------------------------------------------------
 // Memory ordering
 // ---------------------------------------------------------------------------

@@ -1,0 +1,745 @@
+// abx_hierarchy.cu -- Apetrei's bottom-up hierarchy over one or many trees,
+// and the per-tree stages of a batched (forest) build.
+//
+// Trees are segments of one array of Morton-sorted positions: tree s owns
+// positions [off[s], off[s + 1]).  Every formula of GenerateHierarchy
+// (ArborX_TreeConstruction.hpp:71-348) is evaluated in the tree's own
+// numbering: delta() is +inf across a tree boundary and breaks ties of equal
+// codes with the tree-local index, leaves and internal nodes are numbered
+// inside the tree, values are tree-local input indices.  So a tree built in a
+// batch has exactly the node arrays of the same tree built alone.  Storage is
+// global: the internal node with Karras index k (a tree-local position) lives
+// in slot off[s] + k, i.e. at its global sorted position; a one-leaf tree
+// uses slot off[s] for its single traversal node.
+#include <climits>
+
+#include "abx_build.h"
+
+namespace abx
+{
+namespace
+{
+
+// GenerateHierarchy::delta (ArborX_TreeConstruction.hpp:131-170) at global
+// position j of the tree [lo, hi]: xor of adjacent codes; equal codes fall
+// back to LLONG_MIN + (jl ^ (jl + 1)) with the tree-local index jl; the sum is
+// formed in unsigned 64-bit arithmetic and shifted down by one; +inf outside
+// [lo, hi - 1].
+__device__ __forceinline__ long long seg_delta(const uint64_t *__restrict__ codes, int j, int lo,
+                                               int hi)
+{
+  if (j < lo || j >= hi)
+    return LLONG_MAX;
+  const uint64_t x = __ldg(codes + j) ^ __ldg(codes + j + 1);
+  const int jl = j - lo;
+  const uint64_t add =
+      x == 0 ? (0x8000000000000000ull + (uint64_t)(int64_t)(jl ^ (jl + 1))) : 0ull;
+  return (long long)(x + add - 1ull);
+}
+
+// delta at global position j, whatever tree j belongs to.
+__device__ __forceinline__ long long pos_delta(const uint64_t *__restrict__ codes,
+                                               const int64_t *__restrict__ off, int nseg,
+                                               int64_t total, int j)
+{
+  if (j < 0 || (int64_t)j >= total - 1)
+    return LLONG_MAX;
+  const int s = find_segment(off, nseg, j);
+  return seg_delta(codes, j, (int)__ldg(off + s), (int)__ldg(off + s + 1) - 1);
+}
+
+// Count field of a child slot in a TNode: a leaf child is 1; an internal
+// child covering c <= kMaxBucket leaves is c, plus kBucketRightEnd when its
+// Karras index is the right end of its leaf range (its leaves then start at
+// index - c + 1, else at index); larger subtrees are 0.  Query kernels may
+// scan such a child's leaves from the Morton-ordered copy instead of
+// descending into it.
+__device__ __forceinline__ int child_count_field(int kidx, int lo, int hi)
+{
+  const int c = hi - lo + 1;
+  if (c > kMaxBucket)
+    return 0;
+  return c | (kidx == hi ? kBucketRightEnd : 0);
+}
+
+__device__ __forceinline__ Box3 load_internal_box_cg(const InternalNode *node)
+{
+  const float *f = reinterpret_cast<const float *>(node);
+  const float2 a = __ldcg(reinterpret_cast<const float2 *>(f + 2));
+  const float4 b = __ldcg(reinterpret_cast<const float4 *>(f + 4));
+  Box3 r;
+  r.lo[0] = a.x;
+  r.lo[1] = a.y;
+  r.lo[2] = b.x;
+  r.hi[0] = b.y;
+  r.hi[1] = b.z;
+  r.hi[2] = b.w;
+  return r;
+}
+
+// State of a climb that leaves its CTA (handed from k_hierarchy_local to
+// k_hierarchy_global).
+struct __align__(16) ClimbState
+{
+  int range_left, range_right; // global positions
+  int cur_node;                // global slot of the node completed last, -1 for a leaf
+  int node_num;                // its tree-local node number
+  int value;                   // leaf value when cur_node == -1
+  int lo, hi;                  // the tree's positions
+  int pad;
+  float blo[3];
+  float bhi[3];
+  float pad2[2];
+};
+static_assert(sizeof(ClimbState) == 64, "climb state is 64 B");
+
+// The parent created by a climb step.  Writes its 64-byte child-pair node and
+// its reference-layout record; returns its box in `box`.
+struct ParentStep
+{
+  int kp;         // Karras index of the parent (global slot)
+  int left_child; // tree-local node number of its left child
+  int rope;       // tree-local rope
+};
+
+__device__ __forceinline__ void write_parent(TNode *__restrict__ tnodes,
+                                             InternalNode *__restrict__ internal,
+                                             ParentStep const &ps, bool is_left_child, Box3 &box,
+                                             int own_ref, int own_c, Box3 const &sib, int sib_ref,
+                                             int sib_c)
+{
+  tnodes[ps.kp] = is_left_child ? make_tnode(box, own_ref, own_c, sib, sib_ref, sib_c)
+                                : make_tnode(sib, sib_ref, sib_c, box, own_ref, own_c);
+  expand(box, sib);
+  InternalNode node;
+  node.left_child = ps.left_child;
+  node.rope = ps.rope;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    node.lo[d] = box.lo[d];
+    node.hi[d] = box.hi[d];
+  }
+  internal[ps.kp] = node;
+}
+
+// Apetrei's climb with global flags (ArborX_TreeConstruction.hpp:197-311):
+// relaxed compare-and-swap on the parent's range slot; a release fence before
+// it once this thread has written a node record in this kernel (`wrote`;
+// records written by an earlier kernel are already visible); an acquire
+// fence before reading an internal sibling's box through L2.  The first
+// arriver at a parent stops; nothing spins.  Stops at the tree's root.
+template <int KIND>
+__device__ void climb_global(const float *__restrict__ g, const uint32_t *__restrict__ perm,
+                             const uint64_t *__restrict__ codes, int *__restrict__ ranges,
+                             InternalNode *__restrict__ internal, TNode *__restrict__ tnodes,
+                             ClimbState st, bool wrote)
+{
+  const int lo = st.lo, hi = st.hi;
+  const int num_internal = hi - lo; // tree-local
+  int range_left = st.range_left, range_right = st.range_right;
+  int cur_node = st.cur_node, node_num = st.node_num;
+  Box3 box;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    box.lo[d] = st.blo[d];
+    box.hi[d] = st.bhi[d];
+  }
+  long long delta_left = seg_delta(codes, range_left - 1, lo, hi);
+  long long delta_right = seg_delta(codes, range_right, lo, hi);
+  while (!(range_left == lo && range_right == hi))
+  {
+    const bool is_left_child = delta_right < delta_left;
+    const int p = is_left_child ? range_right : range_left - 1;
+    const int own_lo = range_left, own_hi = range_right;
+    if (wrote)
+      fence_acq_rel_gpu(); // release internal[cur_node]
+    const int old = atomic_cas_relaxed(ranges + p, -1, is_left_child ? range_left : range_right);
+    if (old == -1)
+      return;
+    ParentStep ps;
+    int sib_lo, sib_hi;
+    if (is_left_child)
+    {
+      range_right = old;
+      ps.left_child = node_num;
+      sib_lo = p + 1;
+      sib_hi = range_right;
+      delta_right = seg_delta(codes, range_right, lo, hi);
+    }
+    else
+    {
+      range_left = old;
+      ps.left_child = (p == range_left) ? p - lo : p - lo + num_internal + 1;
+      sib_lo = range_left;
+      sib_hi = p;
+      delta_left = seg_delta(codes, range_left - 1, lo, hi);
+    }
+    const int sib_node = is_left_child ? p + 1 : p;
+    const bool sib_leaf = (sib_lo == sib_hi);
+    Box3 sib;
+    int sib_value = 0;
+    if (sib_leaf)
+    {
+      sib_value = (int)__ldg(perm + sib_lo) - lo;
+      sib = load_leaf_box<KIND>(g, sib_value + lo);
+    }
+    else
+    {
+      fence_acq_rel_gpu(); // acquire internal[sib_node]
+      sib = load_internal_box_cg(internal + sib_node);
+    }
+    ps.kp = delta_right < delta_left ? range_right : range_left;
+    if (range_right != hi)
+      ps.rope = delta_right < seg_delta(codes, range_right + 1, lo, hi)
+                    ? range_right + 1 - lo
+                    : range_right + 1 - lo + num_internal + 1;
+    else
+      ps.rope = kRopeSentinel;
+    const int own_ref = cur_node < 0 ? bucket_ref(st.value) : cur_node;
+    const int own_c = cur_node < 0 ? 1 : child_count_field(cur_node, own_lo, own_hi);
+    const int sib_ref = sib_leaf ? bucket_ref(sib_value) : sib_node;
+    const int sib_c = sib_leaf ? 1 : child_count_field(sib_node, sib_lo, sib_hi);
+    write_parent(tnodes, internal, ps, is_left_child, box, own_ref, own_c, sib, sib_ref, sib_c);
+    wrote = true;
+    cur_node = ps.kp;
+    node_num = ps.kp - lo + num_internal + 1;
+  }
+}
+
+// Apetrei's climb, first regime.
+//
+// Each CTA owns kHierBlock consecutive positions [b0, b1].  While the parent a
+// thread climbs to covers only positions of its CTA, the flag exchange and the
+// sibling's box go through shared memory (block-scope fences, no global
+// atomics).  The parent of a node [L, R] lies inside the CTA iff its other
+// child ends inside it: for a left child (split p = R) iff some j in
+// [p + 1, b1] has delta(j) >= delta(p), for a right child (split p = L - 1)
+// iff some j in [b0 - 1, p - 1] has delta(j) > delta(p) -- read from suffix
+// and prefix maxima of the CTA's deltas (tree boundaries have delta = +inf).
+// Both children of a parent reach the same verdict, so they meet on the same
+// flag.  A thread whose parent leaves the CTA records its state in the
+// frontier list and stops, so the CTA retires at once; k_hierarchy_global
+// finishes those climbs (when the list is full the thread finishes its climb
+// with climb_global itself).  Nothing spins: the first arriver at a parent
+// stops.
+//
+// Every internal node gets its reference-layout record and its 64-byte
+// child-pair node; leaf geometry is copied into Morton order on the way.
+template <int KIND>
+__global__ void __launch_bounds__(kHierBlock)
+    k_hierarchy_local(const float *__restrict__ g, int64_t total, const int64_t *__restrict__ off,
+                      int nseg, const uint32_t *__restrict__ perm,
+                      const uint64_t *__restrict__ codes, int *__restrict__ ranges,
+                      LeafNode *__restrict__ leaves, InternalNode *__restrict__ internal,
+                      TNode *__restrict__ tnodes, float4 *__restrict__ sorted,
+                      ClimbState *__restrict__ frontier, unsigned *__restrict__ frontier_count,
+                      int frontier_capacity)
+{
+  __shared__ long long s_delta[kHierBlock + 1]; // delta(b0 - 1 + k)
+  __shared__ long long s_pre[kHierBlock + 1];   // max of s_delta[0 .. k]
+  __shared__ long long s_suf[kHierBlock + 1];   // max of s_delta[k .. nb]
+  __shared__ int s_flag[kHierBlock];            // split p -> s_flag[p - b0]
+  __shared__ Box3 s_box[kHierBlock];           // internal node with slot in [b0, b1]
+  __shared__ Box3 s_leaf[kHierBlock];
+  __shared__ int s_value[kHierBlock];
+
+  const int b0 = blockIdx.x * kHierBlock;
+  const int b1 = (int)min((int64_t)b0 + kHierBlock - 1, total - 1);
+  const int nb = b1 - b0 + 1;
+  const int tid = threadIdx.x;
+
+  for (int k = tid; k <= nb; k += blockDim.x)
+    s_delta[k] = pos_delta(codes, off, nseg, total, b0 - 1 + k);
+  s_flag[tid] = -1;
+  const int i = b0 + tid;
+  Box3 box = empty_box();
+  int value = 0, lo = 0, hi = 0;
+  if (i <= b1)
+  {
+    const int s = nseg > 1 ? find_segment(off, nseg, i) : 0;
+    lo = (int)__ldg(off + s);
+    hi = (int)__ldg(off + s + 1) - 1;
+    const int original = (int)__ldg(perm + i);
+    value = original - lo;
+    box = load_leaf_box<KIND>(g, original);
+    s_leaf[tid] = box;
+    s_value[tid] = value;
+    SortedLeaf<KIND>::store(sorted, i, box, value);
+  }
+  __syncthreads();
+  // inclusive prefix maxima s_pre[k] = max(s_delta[0..k]) and suffix maxima
+  // s_suf[k] = max(s_delta[k..nb]) for k in [0, nb], nb <= kHierBlock:
+  // warp shuffles, then the maxima of the warps before / after
+  {
+    __shared__ long long w_pre[kHierBlock / 32];
+    __shared__ long long w_suf[kHierBlock / 32];
+    const int lane = tid & 31, warp = tid >> 5;
+    const long long v = tid <= nb ? s_delta[tid] : LLONG_MIN;
+    long long pre = v, suf = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+      const long long a = __shfl_up_sync(0xffffffffu, pre, o);
+      const long long b = __shfl_down_sync(0xffffffffu, suf, o);
+      if (lane >= o)
+        pre = max(pre, a);
+      if (lane + o < 32)
+        suf = max(suf, b);
+    }
+    if (lane == 31)
+      w_pre[warp] = pre;
+    if (lane == 0)
+      w_suf[warp] = suf;
+    __syncthreads();
+    for (int w = 0; w < warp; ++w)
+      pre = max(pre, w_pre[w]);
+    for (int w = warp + 1; w < kHierBlock / 32; ++w)
+      suf = max(suf, w_suf[w]);
+    // entry nb = kHierBlock (a full CTA) lies past the last thread
+    const long long last = nb == kHierBlock ? s_delta[kHierBlock] : LLONG_MIN;
+    if (tid <= nb)
+    {
+      s_pre[tid] = pre;
+      s_suf[tid] = max(suf, last);
+    }
+    if (nb == kHierBlock && tid == kHierBlock - 1)
+    {
+      s_pre[kHierBlock] = max(pre, last);
+      s_suf[kHierBlock] = last;
+    }
+    __syncthreads();
+  }
+  if (i > b1)
+    return;
+
+  const int num_internal = hi - lo; // tree-local
+  // delta(j) for j in [b0 - 1, b1]
+  auto delta_at = [&](int j) -> long long { return s_delta[j - b0 + 1]; };
+  // GenerateHierarchy::setRope (ArborX_TreeConstruction.hpp:173-195) in
+  // tree-local node numbers
+  auto rope_of = [&](int range_right, long long delta_right) -> int {
+    if (range_right == hi)
+      return kRopeSentinel;
+    const long long next = range_right + 1 <= b1 ? delta_at(range_right + 1)
+                                                  : seg_delta(codes, range_right + 1, lo, hi);
+    return delta_right < next ? range_right + 1 - lo : range_right + 1 - lo + num_internal + 1;
+  };
+
+  int range_left = i, range_right = i;
+  long long delta_left = delta_at(range_left - 1);
+  long long delta_right = delta_at(range_right);
+  LeafNode leaf;
+  leaf.rope = rope_of(range_right, delta_right);
+  leaf.value = value;
+  leaves[i] = leaf;
+  if (lo == hi)
+  {
+    // one-leaf tree (ArborX_TreeConstruction.hpp:41-69): a one-leaf bucket on
+    // the left, nothing on the right (count 0)
+    tnodes[lo] = make_tnode(box, bucket_ref(value), 1, empty_box(), bucket_ref(0), 0);
+    return;
+  }
+
+  int cur_node = -1;        // slot of the node this thread completed last
+  int node_num = i - lo;    // its tree-local node number
+  while (!(range_left == lo && range_right == hi))
+  {
+    const bool is_left_child = delta_right < delta_left;
+    const int p = is_left_child ? range_right : range_left - 1;
+    const bool inside = is_left_child ? (p < b1 && s_suf[p - b0 + 2] >= delta_right)
+                                      : (p >= b0 && s_pre[p - b0] > delta_left);
+    if (!inside)
+    {
+      ClimbState st;
+      st.range_left = range_left;
+      st.range_right = range_right;
+      st.cur_node = cur_node;
+      st.node_num = node_num;
+      st.value = value;
+      st.lo = lo;
+      st.hi = hi;
+      st.pad = 0;
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+      {
+        st.blo[d] = box.lo[d];
+        st.bhi[d] = box.hi[d];
+      }
+      const unsigned slot = atomicAdd(frontier_count, 1u);
+      if ((int)slot < frontier_capacity)
+        frontier[slot] = st;
+      else // list full (very deep trees): finish this climb here
+        climb_global<KIND>(g, perm, codes, ranges, internal, tnodes, st, cur_node >= 0);
+      return;
+    }
+    const int own_lo = range_left, own_hi = range_right;
+    __threadfence_block(); // release s_box[cur_node - b0]
+    const int old = atomicCAS(s_flag + (p - b0), -1, is_left_child ? range_left : range_right);
+    if (old == -1)
+      return;
+    __threadfence_block(); // acquire the sibling's s_box entry
+    ParentStep ps;
+    int sib_lo, sib_hi;
+    if (is_left_child)
+    {
+      range_right = old;
+      ps.left_child = node_num;
+      sib_lo = p + 1;
+      sib_hi = range_right;
+      delta_right = delta_at(range_right);
+    }
+    else
+    {
+      range_left = old;
+      ps.left_child = (p == range_left) ? p - lo : p - lo + num_internal + 1;
+      sib_lo = range_left;
+      sib_hi = p;
+      delta_left = delta_at(range_left - 1);
+    }
+    const int sib_node = is_left_child ? p + 1 : p;
+    const bool sib_leaf = (sib_lo == sib_hi);
+    const Box3 sib = sib_leaf ? s_leaf[sib_lo - b0] : s_box[sib_node - b0];
+    const int sib_value = sib_leaf ? s_value[sib_lo - b0] : 0;
+    ps.kp = delta_right < delta_left ? range_right : range_left;
+    ps.rope = rope_of(range_right, delta_right);
+    const int own_ref = cur_node < 0 ? bucket_ref(value) : cur_node;
+    const int own_c = cur_node < 0 ? 1 : child_count_field(cur_node, own_lo, own_hi);
+    const int sib_ref = sib_leaf ? bucket_ref(sib_value) : sib_node;
+    const int sib_c = sib_leaf ? 1 : child_count_field(sib_node, sib_lo, sib_hi);
+    write_parent(tnodes, internal, ps, is_left_child, box, own_ref, own_c, sib, sib_ref, sib_c);
+    s_box[ps.kp - b0] = box;
+    cur_node = ps.kp;
+    node_num = ps.kp - lo + num_internal + 1;
+  }
+}
+
+// Second regime: the climbs handed over by k_hierarchy_local.  Their node
+// records were written by the previous kernel.
+template <int KIND>
+__global__ void __launch_bounds__(256)
+    k_hierarchy_global(const float *__restrict__ g, const uint32_t *__restrict__ perm,
+                       const uint64_t *__restrict__ codes, int *__restrict__ ranges,
+                       InternalNode *__restrict__ internal, TNode *__restrict__ tnodes,
+                       const ClimbState *__restrict__ frontier,
+                       const unsigned *__restrict__ frontier_count, int capacity)
+{
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= min((int)*frontier_count, capacity))
+    return;
+  climb_global<KIND>(g, perm, codes, ranges, internal, tnodes, frontier[e], false);
+}
+
+// ---------------------------------------------------------------------------
+// Per-tree stages of a forest build
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ void block_reduce_box(Box3 &b)
+{
+  __shared__ float sh[6][8];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      b.lo[d] = fminf(b.lo[d], __shfl_xor_sync(0xffffffffu, b.lo[d], o));
+      b.hi[d] = fmaxf(b.hi[d], __shfl_xor_sync(0xffffffffu, b.hi[d], o));
+    }
+  }
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+  {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      sh[d][w] = b.lo[d];
+      sh[3 + d][w] = b.hi[d];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    for (int k = 1; k < (int)(blockDim.x >> 5); ++k)
+    {
+#pragma unroll
+      for (int d = 0; d < 3; ++d)
+      {
+        b.lo[d] = fminf(b.lo[d], sh[d][k]);
+        b.hi[d] = fmaxf(b.hi[d], sh[3 + d][k]);
+      }
+    }
+  }
+}
+
+// Bounding box of every tree (one CTA per tree; empty trees get the empty box).
+template <int KIND>
+__global__ void __launch_bounds__(256)
+    k_forest_bounds(const float *__restrict__ g, const int64_t *__restrict__ off,
+                    float *__restrict__ bounds)
+{
+  const int s = blockIdx.x;
+  const int64_t a = off[s], e = off[s + 1];
+  Box3 b = empty_box();
+  for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x)
+    expand(b, load_leaf_box<KIND>(g, i));
+  block_reduce_box(b);
+  if (threadIdx.x == 0)
+  {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+    {
+      bounds[6 * s + d] = b.lo[d];
+      bounds[6 * s + 3 + d] = b.hi[d];
+    }
+  }
+}
+
+__device__ __forceinline__ uint64_t morton64_in(float x, float y, float z, const float *sc)
+{
+  return morton64_unit(translate_scale(x, sc[0], sc[3]), translate_scale(y, sc[1], sc[4]),
+                       translate_scale(z, sc[2], sc[5]));
+}
+
+// Morton64 code of every value against its own tree's box (one CTA per
+// tree), with the 8 digit histograms of the radix sort.
+template <int KIND>
+__global__ void __launch_bounds__(256)
+    k_forest_morton64(const float *__restrict__ g, const int64_t *__restrict__ off,
+                      const float *__restrict__ bounds, uint64_t *__restrict__ codes,
+                      uint32_t *__restrict__ hist)
+{
+  __shared__ uint32_t sh[8 * 256];
+  __shared__ float sc[6];
+  const int s = blockIdx.x;
+  for (int k = threadIdx.x; k < 8 * 256; k += blockDim.x)
+    sh[k] = 0;
+  if (threadIdx.x < 6)
+    sc[threadIdx.x] = bounds[6 * s + threadIdx.x];
+  __syncthreads();
+  const int64_t a = off[s], e = off[s + 1];
+  for (int64_t i = a + threadIdx.x; i < e; i += blockDim.x)
+  {
+    float x, y, z;
+    load_centroid<KIND>(g, i, x, y, z);
+    const uint64_t c = morton64_in(x, y, z, sc);
+    codes[i] = c;
+#pragma unroll
+    for (int p = 0; p < 8; ++p)
+      atomicAdd(&sh[p * 256 + ((c >> (8 * p)) & 0xff)], 1u);
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < 8 * 256; k += blockDim.x)
+    if (sh[k])
+      atomicAdd(&hist[k], sh[k]);
+}
+
+// keys[i] = tree of the value at sorted position i.
+__global__ void k_tree_keys(const uint32_t *__restrict__ perm, const int64_t *__restrict__ off,
+                            int nseg, int64_t total, uint32_t *__restrict__ keys)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < total)
+    keys[i] = (uint32_t)find_segment(off, nseg, perm[i]);
+}
+
+// Morton64 code of the value at every sorted position (after the regroup by
+// tree), recomputed with the same arithmetic as k_forest_morton64.
+template <int KIND>
+__global__ void k_forest_codes(const float *__restrict__ g, const uint32_t *__restrict__ perm,
+                               const int64_t *__restrict__ off, int nseg, int64_t total,
+                               const float *__restrict__ bounds, uint64_t *__restrict__ codes)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total)
+    return;
+  const int s = find_segment(off, nseg, i);
+  float sc[6];
+#pragma unroll
+  for (int d = 0; d < 6; ++d)
+    sc[d] = __ldg(bounds + 6 * s + d);
+  float x, y, z;
+  load_centroid<KIND>(g, perm[i], x, y, z);
+  codes[i] = morton64_in(x, y, z, sc);
+}
+
+// Predicate ordering key of a forest query: its tree above the Morton32 code
+// of its centroid in that tree's box (ArborX_LinearBVH.hpp:287-306 per tree).
+template <int KIND>
+__global__ void k_forest_query_keys(const float *__restrict__ preds,
+                                    const int64_t *__restrict__ qoff, int nseg, int64_t nq,
+                                    const float *__restrict__ bounds, uint64_t *__restrict__ keys)
+{
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nq)
+    return;
+  const int s = find_segment(qoff, nseg, q);
+  const float *sc = bounds + 6 * s;
+  float x, y, z;
+  load_centroid<KIND>(preds, q, x, y, z);
+  const uint32_t c = morton32_unit(translate_scale(x, __ldg(sc), __ldg(sc + 3)),
+                                   translate_scale(y, __ldg(sc + 1), __ldg(sc + 4)),
+                                   translate_scale(z, __ldg(sc + 2), __ldg(sc + 5)));
+  keys[q] = ((uint64_t)s << 32) | c;
+}
+
+__global__ void k_one_segment(int64_t *off, int64_t n)
+{
+  off[0] = 0;
+  off[1] = n;
+}
+
+} // namespace
+
+abx_status generate_hierarchy_segments(cudaStream_t s, abx_geometry kind, const float *d_g,
+                                       int64_t total, const int64_t *d_off, int nseg,
+                                       const uint32_t *d_perm, const uint64_t *d_codes,
+                                       LeafNode *d_leaves, InternalNode *d_internal,
+                                       TNode *d_tnodes, float4 *d_sorted)
+{
+  if (total < 1)
+    return ABX_SUCCESS;
+  if (total > (int64_t)INT32_MAX / 2)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "generate_hierarchy: too many values");
+  Scratch<int> ranges;
+  ABX_CUDA_TRY(ranges.alloc(total, s));
+  ABX_CUDA_TRY(cudaMemsetAsync(ranges.ptr, 0xff, sizeof(int) * total, s));
+  Scratch<float4> tmp_sorted;
+  if (!d_sorted)
+  {
+    ABX_CUDA_TRY(tmp_sorted.alloc((size_t)total * (kind == ABX_BOX ? 2 : 1), s));
+    d_sorted = tmp_sorted.ptr;
+  }
+  const unsigned blocks = (unsigned)((total + kHierBlock - 1) / kHierBlock);
+  // a CTA's positions split into a few maximal subtrees (2 log2(512) + 2 for
+  // a balanced tree), each handing over at most one climb; deeper trees that
+  // overflow the list finish those climbs in the first kernel
+  const int capacity = (int)blocks * 24;
+  Scratch<ClimbState> frontier;
+  Scratch<unsigned> count;
+  ABX_CUDA_TRY(frontier.alloc((size_t)capacity, s));
+  ABX_CUDA_TRY(count.alloc(1, s));
+  ABX_CUDA_TRY(cudaMemsetAsync(count.ptr, 0, sizeof(unsigned), s));
+  const unsigned gblocks = (unsigned)((capacity + 255) / 256);
+  StageScope scope(s, "hierarchy", 2);
+  if (kind == ABX_POINT)
+  {
+    k_hierarchy_local<0><<<blocks, kHierBlock, 0, s>>>(
+        d_g, total, d_off, nseg, d_perm, d_codes, ranges.ptr, d_leaves, d_internal, d_tnodes,
+        d_sorted, frontier.ptr, count.ptr, capacity);
+    k_hierarchy_global<0><<<gblocks, 256, 0, s>>>(d_g, d_perm, d_codes, ranges.ptr, d_internal,
+                                                  d_tnodes, frontier.ptr, count.ptr, capacity);
+  }
+  else
+  {
+    k_hierarchy_local<1><<<blocks, kHierBlock, 0, s>>>(
+        d_g, total, d_off, nseg, d_perm, d_codes, ranges.ptr, d_leaves, d_internal, d_tnodes,
+        d_sorted, frontier.ptr, count.ptr, capacity);
+    k_hierarchy_global<1><<<gblocks, 256, 0, s>>>(d_g, d_perm, d_codes, ranges.ptr, d_internal,
+                                                  d_tnodes, frontier.ptr, count.ptr, capacity);
+  }
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
+
+abx_status generate_hierarchy(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
+                              const uint32_t *d_perm, const uint64_t *d_codes,
+                              LeafNode *d_leaves, InternalNode *d_internal, TNode *d_tnodes,
+                              float4 *d_sorted)
+{
+  if (n < 2)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "generate_hierarchy needs at least 2 values");
+  Scratch<TNode> tmp_t;
+  if (!d_tnodes)
+  {
+    ABX_CUDA_TRY(tmp_t.alloc(n, s));
+    d_tnodes = tmp_t.ptr;
+  }
+  Scratch<int64_t> off;
+  ABX_CUDA_TRY(off.alloc(2, s));
+  k_one_segment<<<1, 1, 0, s>>>(off.ptr, n);
+  return generate_hierarchy_segments(s, kind, d_g, n, off.ptr, 1, d_perm, d_codes, d_leaves,
+                                     d_internal, d_tnodes, d_sorted);
+}
+
+abx_status forest_build(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t total,
+                        const int64_t *d_off, int nseg, float *d_bounds, LeafNode *d_leaves,
+                        InternalNode *d_internal, TNode *d_tnodes, float4 *d_sorted)
+{
+  if (nseg < 1)
+    return ABX_SUCCESS;
+  {
+    StageScope scope(s, "bounds", 1);
+    if (kind == ABX_POINT)
+      k_forest_bounds<0><<<nseg, 256, 0, s>>>(d_g, d_off, d_bounds);
+    else
+      k_forest_bounds<1><<<nseg, 256, 0, s>>>(d_g, d_off, d_bounds);
+    ABX_CUDA_TRY(cudaGetLastError());
+  }
+  if (total < 1)
+    return ABX_SUCCESS;
+  Scratch<uint64_t> codes;
+  Scratch<uint32_t> perm, perm2, keys, hist;
+  ABX_CUDA_TRY(codes.alloc(total, s));
+  ABX_CUDA_TRY(perm.alloc(total, s));
+  ABX_CUDA_TRY(hist.alloc(8 * 256, s));
+  ABX_CUDA_TRY(cudaMemsetAsync(hist.ptr, 0, 8 * 256 * sizeof(uint32_t), s));
+  {
+    StageScope scope(s, "morton64", 1);
+    if (kind == ABX_POINT)
+      k_forest_morton64<0><<<nseg, 256, 0, s>>>(d_g, d_off, d_bounds, codes.ptr, hist.ptr);
+    else
+      k_forest_morton64<1><<<nseg, 256, 0, s>>>(d_g, d_off, d_bounds, codes.ptr, hist.ptr);
+    ABX_CUDA_TRY(cudaGetLastError());
+  }
+  // stable by code over all trees, then stable by tree: a stable sort of
+  // every tree by its own codes
+  ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, total, 8, hist.ptr));
+  const uint32_t *final_perm = perm.ptr;
+  int tree_bits = 0;
+  while ((1ll << tree_bits) < nseg)
+    ++tree_bits;
+  if (tree_bits > 0)
+  {
+    ABX_CUDA_TRY(perm2.alloc(total, s));
+    ABX_CUDA_TRY(keys.alloc(total, s));
+    const unsigned blocks = (unsigned)((total + 255) / 256);
+    k_tree_keys<<<blocks, 256, 0, s>>>(perm.ptr, d_off, nseg, total, keys.ptr);
+    ABX_TRY(radix_sort_u32(s, keys.ptr, perm2.ptr, perm.ptr, total, (tree_bits + 7) / 8, nullptr));
+    final_perm = perm2.ptr;
+    if (kind == ABX_POINT)
+      k_forest_codes<0><<<blocks, 256, 0, s>>>(d_g, final_perm, d_off, nseg, total, d_bounds,
+                                               codes.ptr);
+    else
+      k_forest_codes<1><<<blocks, 256, 0, s>>>(d_g, final_perm, d_off, nseg, total, d_bounds,
+                                               codes.ptr);
+    ABX_CUDA_TRY(cudaGetLastError());
+  }
+  return generate_hierarchy_segments(s, kind, d_g, total, d_off, nseg, final_perm, codes.ptr,
+                                     d_leaves, d_internal, d_tnodes, d_sorted);
+}
+
+abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const float *d_preds,
+                              int64_t nq, const int64_t *d_qoff, int nseg,
+                              const float *d_bounds, uint32_t *d_perm)
+{
+  if (nq < 1)
+    return ABX_SUCCESS;
+  Scratch<uint64_t> keys;
+  ABX_CUDA_TRY(keys.alloc(nq, s));
+  const unsigned blocks = (unsigned)((nq + 255) / 256);
+  if (pred_kind == ABX_POINT)
+    k_forest_query_keys<0><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, nq, d_bounds, keys.ptr);
+  else if (pred_kind == ABX_BOX)
+    k_forest_query_keys<1><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, nq, d_bounds, keys.ptr);
+  else
+    k_forest_query_keys<2><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, nq, d_bounds, keys.ptr);
+  ABX_CUDA_TRY(cudaGetLastError());
+  int tree_bits = 0;
+  while ((1ll << tree_bits) < nseg)
+    ++tree_bits;
+  return radix_sort_u64(s, keys.ptr, d_perm, nullptr, nq, (32 + tree_bits + 7) / 8, nullptr);
+}
+
+} // namespace abx

@@ -32,6 +32,23 @@ namespace
 
 constexpr int kQueryThreads = 128;
 
+// The tree a query runs on: root node slot and number of leaves (a forest
+// query finds its tree from the query offsets).
+struct QueryTree
+{
+  int root;
+  int64_t size;
+};
+
+__device__ __forceinline__ QueryTree query_tree(int64_t q, int64_t n, ForestView const &f)
+{
+  if (!f.qoff)
+    return QueryTree{0, n};
+  const int s = find_segment(f.qoff, f.nseg, q);
+  const int64_t lo = __ldg(f.tree_off + s);
+  return QueryTree{(int)lo, __ldg(f.tree_off + s + 1) - lo};
+}
+
 __device__ __forceinline__ TNode load_tnode(const TNode *__restrict__ nodes, int i)
 {
   const float4 *p = reinterpret_cast<const float4 *>(nodes + i);
@@ -171,15 +188,22 @@ __device__ __forceinline__ ChildKind child_kind(int ref, int cf, int bucket, int
 template <int PRED, int MODE, int KIND>
 __global__ void __launch_bounds__(kQueryThreads)
     k_spatial(const TNode *__restrict__ nodes, const float4 *__restrict__ sorted, int64_t n,
-              const float *__restrict__ preds, int64_t nq, const uint32_t *__restrict__ perm,
-              int32_t *__restrict__ counts, const int32_t *__restrict__ offsets,
-              int32_t *__restrict__ out, int32_t buffer, int bucket,
-              unsigned *__restrict__ overflow, unsigned *__restrict__ err)
+              ForestView f, const float *__restrict__ preds, int64_t nq,
+              const uint32_t *__restrict__ perm, int32_t *__restrict__ counts,
+              const int32_t *__restrict__ offsets, int32_t *__restrict__ out, int32_t buffer,
+              int bucket, unsigned *__restrict__ overflow, unsigned *__restrict__ err)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nq)
     return;
   const int64_t q = perm ? (int64_t)__ldg(perm + t) : t;
+  const QueryTree tree = query_tree(q, n, f);
+  if (tree.size <= 0)
+  {
+    if (MODE != kFill)
+      counts[q] = 0;
+    return;
+  }
   const auto pred = PredOf<PRED>::load(preds, q);
 
   int32_t *dst = nullptr;
@@ -225,12 +249,12 @@ __global__ void __launch_bounds__(kQueryThreads)
   int sref[kStackDepth];
   int scf[kStackDepth];
   int sp = 0;
-  int node = 0;
-  const int64_t num_nodes = n > 1 ? n - 1 : 1;
+  int node = tree.root;
+  const int64_t num_nodes = tree.size > 1 ? tree.size - 1 : 1;
   int64_t budget = num_nodes; // a depth-first walk visits each node at most once
   while (true)
   {
-    if (--budget < 0 || (uint64_t)node >= (uint64_t)num_nodes)
+    if (--budget < 0 || (uint64_t)(node - tree.root) >= (uint64_t)num_nodes)
     {
       raise_error(err, ABX_DEVERR_INTERNAL);
       break;
@@ -342,7 +366,8 @@ struct KnnTask
   int64_t base;
 };
 
-__device__ __forceinline__ KnnTask knn_task(int64_t t, int64_t n, int64_t nq,
+__device__ __forceinline__ KnnTask knn_task(int64_t t, int64_t n, ForestView const &f,
+                                            QueryTree &tree, int64_t nq,
                                             const uint32_t *__restrict__ perm,
                                             const int32_t *__restrict__ kq, int32_t k_all,
                                             const int32_t *__restrict__ offsets,
@@ -350,6 +375,8 @@ __device__ __forceinline__ KnnTask knn_task(int64_t t, int64_t n, int64_t nq,
 {
   KnnTask task;
   task.q = perm ? (int64_t)__ldg(perm + t) : t;
+  tree = query_tree(task.q, n, f);
+  n = tree.size;
   const int k = kq ? __ldg(kq + task.q) : k_all;
   task.k = k < 0 ? 0 : k;
   task.kk = (int)((int64_t)task.k < n ? (int64_t)task.k : n);
@@ -373,7 +400,8 @@ __device__ __forceinline__ KnnTask knn_task(int64_t t, int64_t n, int64_t nq,
 template <int K, int KIND, bool SCAN>
 __global__ void __launch_bounds__(kQueryThreads)
     k_nearest(const TNode *__restrict__ nodes, const float4 *__restrict__ sorted, int64_t n,
-              const float *__restrict__ queries, int64_t nq, const uint32_t *__restrict__ perm,
+              ForestView f, const float *__restrict__ queries, int64_t nq,
+              const uint32_t *__restrict__ perm,
               const int32_t *__restrict__ kq, int32_t k_all, const int32_t *__restrict__ offsets,
               int32_t *__restrict__ offsets_out, int32_t *__restrict__ out_idx,
               float *__restrict__ out_dist, int bucket, unsigned *__restrict__ err)
@@ -381,7 +409,8 @@ __global__ void __launch_bounds__(kQueryThreads)
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nq)
     return;
-  const KnnTask task = knn_task(t, n, nq, perm, kq, k_all, offsets, offsets_out);
+  QueryTree tree;
+  const KnnTask task = knn_task(t, n, f, tree, nq, perm, kq, k_all, offsets, offsets_out);
   if (task.kk == 0)
     return;
   uint64_t key[K];
@@ -429,12 +458,12 @@ __global__ void __launch_bounds__(kQueryThreads)
   int sref[kStackDepth];
   float sdist[kStackDepth];
   int sp = 0;
-  int node = 0;
-  const int64_t num_nodes = n > 1 ? n - 1 : 1;
+  int node = tree.root;
+  const int64_t num_nodes = tree.size > 1 ? tree.size - 1 : 1;
   int64_t budget = num_nodes;
   while (true)
   {
-    if (--budget < 0 || (uint64_t)node >= (uint64_t)num_nodes)
+    if (--budget < 0 || (uint64_t)(node - tree.root) >= (uint64_t)num_nodes)
     {
       raise_error(err, ABX_DEVERR_INTERNAL);
       break;
@@ -544,7 +573,7 @@ __device__ void heap_push(float *hd, int *hi, int &size, float d, int v)
 template <int KIND>
 __global__ void __launch_bounds__(kQueryThreads)
     k_nearest_large(const TNode *__restrict__ nodes, const float4 *__restrict__ sorted,
-                    int64_t n, const float *__restrict__ queries, int64_t nq,
+                    int64_t n, ForestView f, const float *__restrict__ queries, int64_t nq,
                     const uint32_t *__restrict__ perm, const int32_t *__restrict__ kq,
                     int32_t k_all, const int32_t *__restrict__ offsets,
                     int32_t *__restrict__ offsets_out, int32_t *__restrict__ out_idx,
@@ -553,7 +582,8 @@ __global__ void __launch_bounds__(kQueryThreads)
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nq)
     return;
-  const KnnTask task = knn_task(t, n, nq, perm, kq, k_all, offsets, offsets_out);
+  QueryTree tree;
+  const KnnTask task = knn_task(t, n, f, tree, nq, perm, kq, k_all, offsets, offsets_out);
   const int kk = task.kk;
   if (kk == 0)
     return;
@@ -597,12 +627,12 @@ __global__ void __launch_bounds__(kQueryThreads)
   int sref[kStackDepth];
   float sdist[kStackDepth];
   int sp = 0;
-  int node = 0;
-  const int64_t num_nodes = n > 1 ? n - 1 : 1;
+  int node = tree.root;
+  const int64_t num_nodes = tree.size > 1 ? tree.size - 1 : 1;
   int64_t budget = num_nodes;
   while (true)
   {
-    if (--budget < 0 || (uint64_t)node >= (uint64_t)num_nodes)
+    if (--budget < 0 || (uint64_t)(node - tree.root) >= (uint64_t)num_nodes)
     {
       raise_error(err, ABX_DEVERR_INTERNAL);
       break;
@@ -664,16 +694,17 @@ __global__ void __launch_bounds__(kQueryThreads)
   }
 }
 
-__global__ void k_knn_counts(const int32_t *__restrict__ kq, int64_t nq, int64_t n,
-                             int32_t *__restrict__ counts, int32_t *__restrict__ kmax)
+__global__ void k_knn_counts(int64_t n, ForestView f, const int32_t *__restrict__ kq, int32_t k_all,
+                             int64_t nq, int32_t *__restrict__ counts, int32_t *__restrict__ kmax)
 {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int32_t m = 0;
   if (i < nq)
   {
-    int32_t k = kq[i];
+    int32_t k = kq ? kq[i] : k_all;
     k = k < 0 ? 0 : k;
-    counts[i] = (int32_t)((int64_t)k < n ? (int64_t)k : n);
+    const int64_t size = query_tree(i, n, f).size;
+    counts[i] = (int32_t)((int64_t)k < size ? (int64_t)k : size);
     m = k;
   }
 #pragma unroll
@@ -688,7 +719,8 @@ __global__ void k_knn_counts(const int32_t *__restrict__ kq, int64_t nq, int64_t
 // ---------------------------------------------------------------------------
 
 template <int PRED, int KIND>
-abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, const float *d_preds,
+abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, ForestView const &f,
+                            const float *d_preds,
                             int64_t nq, const uint32_t *d_perm, SpatialMode mode,
                             int32_t *d_counts, const int32_t *d_offsets, int32_t *d_out,
                             int32_t buffer, unsigned *d_overflow)
@@ -698,7 +730,7 @@ abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, const float *d_pr
   const int bucket =
       std::max(1, std::min(kMaxBucket, tuning_value("SPATIAL_BUCKET", kDefaultSpatialBucket)));
 #define ABX_SPATIAL(M)                                                                      \
-  k_spatial<PRED, M, KIND><<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.sorted, t.n, d_preds, \
+  k_spatial<PRED, M, KIND><<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.sorted, t.n, f, d_preds, \
                                                             nq, d_perm, d_counts, d_offsets,  \
                                                             d_out, buffer, bucket, d_overflow, \
                                                             err)
@@ -714,7 +746,8 @@ abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, const float *d_pr
 }
 
 template <int K, int KIND>
-abx_status nearest_k(cudaStream_t s, TreeView const &t, const float *d_queries, int64_t nq,
+abx_status nearest_k(cudaStream_t s, TreeView const &t, ForestView const &f,
+                     const float *d_queries, int64_t nq,
                      const uint32_t *d_perm, const int32_t *d_k, int32_t k,
                      const int32_t *d_offsets, int32_t *d_offsets_out, int32_t *d_idx,
                      float *d_dist, unsigned *err)
@@ -724,25 +757,26 @@ abx_status nearest_k(cudaStream_t s, TreeView const &t, const float *d_queries, 
       std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
   if (bucket >= 2)
     k_nearest<K, KIND, true><<<blocks, kQueryThreads, 0, s>>>(
-        t.tnodes, t.sorted, t.n, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, d_idx,
+        t.tnodes, t.sorted, t.n, f, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, d_idx,
         d_dist, bucket, err);
   else
     k_nearest<K, KIND, false><<<blocks, kQueryThreads, 0, s>>>(
-        t.tnodes, t.sorted, t.n, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, d_idx,
+        t.tnodes, t.sorted, t.n, f, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, d_idx,
         d_dist, bucket, err);
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
 }
 
 template <int KIND>
-abx_status nearest_dispatch(cudaStream_t s, TreeView const &t, const float *d_queries,
+abx_status nearest_dispatch(cudaStream_t s, TreeView const &t, ForestView const &f,
+                            const float *d_queries,
                             int64_t nq, const uint32_t *d_perm, const int32_t *d_k, int32_t k,
                             int32_t max_k, const int32_t *d_offsets, int32_t *d_offsets_out,
                             int32_t *d_idx, float *d_dist)
 {
   unsigned *err = device_state().d_error;
 #define ABX_KNN(KV)                                                                             \
-  return nearest_k<KV, KIND>(s, t, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, \
+  return nearest_k<KV, KIND>(s, t, f, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, \
                              d_idx, d_dist, err)
   if (max_k <= 1)
     ABX_KNN(1);
@@ -760,7 +794,7 @@ abx_status nearest_dispatch(cudaStream_t s, TreeView const &t, const float *d_qu
   const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
   const int bucket =
       std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
-  k_nearest_large<KIND><<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.sorted, t.n, d_queries, nq,
+  k_nearest_large<KIND><<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.sorted, t.n, f, d_queries, nq,
                                                          d_perm, d_k, k, d_offsets,
                                                          d_offsets_out, d_idx, d_dist, bucket,
                                                          err);
@@ -770,24 +804,26 @@ abx_status nearest_dispatch(cudaStream_t s, TreeView const &t, const float *d_qu
 
 } // namespace
 
-abx_status launch_spatial(cudaStream_t s, TreeView const &t, abx_geometry pred_kind,
-                          const float *d_preds, int64_t nq, const uint32_t *d_perm,
-                          SpatialMode mode, int32_t *d_counts, const int32_t *d_offsets,
-                          int32_t *d_out, int32_t buffer, unsigned *d_overflow)
+abx_status launch_spatial(cudaStream_t s, TreeView const &t, ForestView const *fp,
+                          abx_geometry pred_kind, const float *d_preds, int64_t nq,
+                          const uint32_t *d_perm, SpatialMode mode, int32_t *d_counts,
+                          const int32_t *d_offsets, int32_t *d_out, int32_t buffer,
+                          unsigned *d_overflow)
 {
   if (nq <= 0 || t.n <= 0)
     return ABX_SUCCESS;
+  const ForestView f = fp ? *fp : ForestView{nullptr, nullptr, 1};
   StageScope scope(s, "spatial", 1);
   const bool box_leaves = t.kind == ABX_BOX;
   if (pred_kind == ABX_SPHERE)
-    return box_leaves ? spatial_dispatch<ABX_SPHERE, 1>(s, t, d_preds, nq, d_perm, mode, d_counts,
+    return box_leaves ? spatial_dispatch<ABX_SPHERE, 1>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
                                                         d_offsets, d_out, buffer, d_overflow)
-                      : spatial_dispatch<ABX_SPHERE, 0>(s, t, d_preds, nq, d_perm, mode, d_counts,
+                      : spatial_dispatch<ABX_SPHERE, 0>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
                                                         d_offsets, d_out, buffer, d_overflow);
   if (pred_kind == ABX_BOX)
-    return box_leaves ? spatial_dispatch<ABX_BOX, 1>(s, t, d_preds, nq, d_perm, mode, d_counts,
+    return box_leaves ? spatial_dispatch<ABX_BOX, 1>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
                                                      d_offsets, d_out, buffer, d_overflow)
-                      : spatial_dispatch<ABX_BOX, 0>(s, t, d_preds, nq, d_perm, mode, d_counts,
+                      : spatial_dispatch<ABX_BOX, 0>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
                                                      d_offsets, d_out, buffer, d_overflow);
   return fail(ABX_ERROR_INVALID_ARGUMENT, "intersects predicates must be spheres or boxes");
 }
@@ -804,29 +840,32 @@ abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int3
   return ABX_SUCCESS;
 }
 
-abx_status launch_nearest(cudaStream_t s, TreeView const &t, const float *d_queries,
-                          int64_t nq, const uint32_t *d_perm, const int32_t *d_k,
-                          int32_t k, int32_t max_k, const int32_t *d_offsets,
+abx_status launch_nearest(cudaStream_t s, TreeView const &t, ForestView const *fp,
+                          const float *d_queries, int64_t nq, const uint32_t *d_perm,
+                          const int32_t *d_k, int32_t k, int32_t max_k, const int32_t *d_offsets,
                           int32_t *d_offsets_out, int32_t *d_idx, float *d_dist)
 {
   if (nq <= 0)
     return ABX_SUCCESS;
+  const ForestView f = fp ? *fp : ForestView{nullptr, nullptr, 1};
   StageScope scope(s, "nearest", 1);
   if (t.kind == ABX_BOX)
-    return nearest_dispatch<1>(s, t, d_queries, nq, d_perm, d_k, k, max_k, d_offsets,
+    return nearest_dispatch<1>(s, t, f, d_queries, nq, d_perm, d_k, k, max_k, d_offsets,
                                d_offsets_out, d_idx, d_dist);
-  return nearest_dispatch<0>(s, t, d_queries, nq, d_perm, d_k, k, max_k, d_offsets,
+  return nearest_dispatch<0>(s, t, f, d_queries, nq, d_perm, d_k, k, max_k, d_offsets,
                              d_offsets_out, d_idx, d_dist);
 }
 
-abx_status launch_knn_counts(cudaStream_t s, const int32_t *d_k, int64_t nq, int64_t n,
-                             int32_t *d_counts, int32_t *d_max)
+abx_status launch_knn_counts(cudaStream_t s, TreeView const &t, ForestView const *fp,
+                             const int32_t *d_k, int32_t k, int64_t nq, int32_t *d_counts,
+                             int32_t *d_max)
 {
   if (nq <= 0)
     return ABX_SUCCESS;
+  const ForestView f = fp ? *fp : ForestView{nullptr, nullptr, 1};
   const unsigned blocks = (unsigned)((nq + 255) / 256);
   StageScope scope(s, "knn_counts", 1);
-  k_knn_counts<<<blocks, 256, 0, s>>>(d_k, nq, n, d_counts, d_max);
+  k_knn_counts<<<blocks, 256, 0, s>>>(t.n, f, d_k, k, nq, d_counts, d_max);
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
 }

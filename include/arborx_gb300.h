@@ -51,6 +51,7 @@ typedef enum abx_status
 
 typedef struct abx_bvh abx_bvh; /* opaque tree                                */
 typedef struct abx_crs abx_crs; /* opaque CRS result (offsets + indices)      */
+typedef struct abx_forest abx_forest; /* opaque batch of independent trees    */
 
 /* Geometry of values and predicates, float32, array-of-structures:
  *   POINT  x y z                 (12 bytes)   ArborX::Point<3>
@@ -211,6 +212,55 @@ ABX_API abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream,
                                  const int32_t *d_k, int32_t k,
                                  abx_traversal_policy policy,
                                  int32_t with_distances, abx_crs **out);
+
+/* ---------------------------------------------------------------------- */
+/* Batched trees (forest)                                                 */
+/* ---------------------------------------------------------------------- */
+/* Replaces the many-trees pattern of the reference
+ * (benchmarks/execution_space_instances/execution_space_instances_driver.cpp:
+ * 187-233: one BoundingVolumeHierarchy per subview of a values array, each
+ * built and queried through its own call) by one build and one query launch
+ * sequence over all trees.  Tree t holds the values
+ * d_values[h_offsets[t] .. h_offsets[t + 1]) (h_offsets: host, ntrees + 1
+ * entries, h_offsets[0] = 0, non-decreasing; empty trees allowed).  Each tree
+ * is exactly the tree abx_bvh_create builds from its subview alone: same
+ * scene box, node arrays (abx_forest_export_nodes), tree-local values. */
+ABX_API abx_status abx_forest_create(void *stream, abx_geometry kind,
+                                     const float *d_values,
+                                     const int64_t *h_offsets, int32_t ntrees,
+                                     abx_forest **out);
+ABX_API abx_status abx_forest_destroy(abx_forest *forest);
+ABX_API int32_t abx_forest_num_trees(const abx_forest *forest);
+/* Number of values in tree `tree` (0 for a bad index). */
+ABX_API int64_t abx_forest_size(const abx_forest *forest, int32_t tree);
+/* Bounds of one tree (ArborX_LinearBVH.hpp:104): 6 host floats. */
+ABX_API abx_status abx_forest_bounds(const abx_forest *forest, int32_t tree,
+                                     float h_box[6]);
+/* The node arrays of one tree, in the layout of abx_bvh_export_nodes. */
+ABX_API abx_status abx_forest_export_nodes(const abx_forest *forest,
+                                           int32_t tree, void *stream,
+                                           int32_t *d_leaves, void *d_internal);
+
+/* Queries grouped by tree: the predicates
+ * d_predicates[h_query_offsets[t] .. h_query_offsets[t + 1]) run on tree t
+ * (h_query_offsets: host, ntrees + 1 entries).  One CRS result over all
+ * queries; its indices are tree-local values, so query q of tree t returns
+ * what abx_bvh_query_intersects / abx_bvh_query_nearest on tree t alone
+ * return for it, in the same order.  Both calls synchronise `stream` once. */
+ABX_API abx_status abx_forest_query_intersects(const abx_forest *forest,
+                                               void *stream, abx_geometry kind,
+                                               const float *d_predicates,
+                                               const int64_t *h_query_offsets,
+                                               abx_traversal_policy policy,
+                                               abx_crs **out);
+ABX_API abx_status abx_forest_query_nearest(const abx_forest *forest,
+                                            void *stream,
+                                            const float *d_queries,
+                                            const int64_t *h_query_offsets,
+                                            const int32_t *d_k, int32_t k,
+                                            abx_traversal_policy policy,
+                                            int32_t with_distances,
+                                            abx_crs **out);
 
 /* Accessors of a CRS result: device offsets (nq + 1), device indices
  * (num_results), device distances (nearest only, else NULL). */

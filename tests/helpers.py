@@ -88,3 +88,26 @@ def manufactured_grid(nx=11, L=100.0, seed=0):
 def uniform_points(n, seed):
     rng = np.random.default_rng(seed)
     return rng.random((n, 3), dtype=np.float32)
+
+
+def clouds(sizes, seed):
+    """Point clouds of the batched workload's shape: cloud i has a lower
+    corner in [0, 100)^3, extents 10^U(-1, 1) per axis and sizes[i] points
+    uniform in its box.  Returns (points [N,3] f32, offsets [ntrees+1])."""
+    rng = np.random.default_rng(seed)
+    sizes = np.asarray(sizes, np.int64)
+    corner = rng.uniform(0, 100, (sizes.size, 3)).astype(np.float32)
+    extent = (10.0 ** rng.uniform(-1, 1, (sizes.size, 3))).astype(np.float32)
+    parts = [corner[i] + extent[i] * rng.random((s, 3), dtype=np.float32)
+             for i, s in enumerate(sizes)]
+    pts = np.concatenate(parts).astype(np.float32) if parts else np.zeros((0, 3), np.float32)
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    return pts, offsets, extent
+
+
+def cloud_box_queries(pts, offsets, extent, frac=0.02):
+    """One axis-aligned box per point, centred on it, full edge frac x its
+    cloud's extent per axis."""
+    tree = np.repeat(np.arange(offsets.size - 1), np.diff(offsets))
+    half = (0.5 * frac * extent[tree]).astype(np.float32)
+    return np.concatenate([pts - half, pts + half], axis=1).astype(np.float32)

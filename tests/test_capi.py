@@ -46,3 +46,23 @@ def test_python_binding_covers_header(libpath):
     assert L.abx_status_string(4) == b"ABX_ERROR_BUFFER_OVERFLOW"
     assert L.abx_version().decode().count(".") == 2
 
+
+
+def test_forest_arguments_are_checked_on_the_host():
+    """Bad forest offsets are refused before any device work (no GPU needed)."""
+    import ctypes
+
+    import numpy as np
+
+    from arborx_gb300 import _lib
+
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    for offsets in ([1, 5], [0, 6, 5], [0, -1]):
+        o = np.asarray(offsets, np.int64)
+        st = L.abx_forest_create(None, 0, ctypes.c_void_p(16), o.ctypes.data, o.size - 1, ctypes.byref(h))
+        assert st == 1 and not h.value  # ABX_ERROR_INVALID_ARGUMENT
+    o = np.asarray([0], np.int64)
+    assert L.abx_forest_create(None, 0, None, o.ctypes.data, 0, ctypes.byref(h)) == 1
+    assert L.abx_forest_create(None, 2, None, o.ctypes.data, 0, ctypes.byref(h)) == 1
+    assert L.abx_forest_num_trees(None) == 0 and L.abx_forest_size(None, 0) == 0
