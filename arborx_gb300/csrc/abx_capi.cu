@@ -274,7 +274,8 @@ abx_status build_tree(abx_bvh *t, const float *d_values)
     // computed straight into the tree bounds
     ABX_TRY(scene_bounds(s, t->kind, d_values, n, t->d_bounds));
     ABX_TRY(morton64_codes(s, t->kind, d_values, n, t->d_bounds, codes.ptr, hist.ptr));
-    ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, n, 8, hist.ptr));
+    ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, n, 8, hist.ptr,
+                           hybrid_top_passes(n, 8)));
     ABX_TRY(generate_hierarchy(s, t->kind, d_values, n, perm.ptr, codes.ptr, t->leaves,
                                t->internal, t->tnodes, t->sorted));
   }
@@ -326,7 +327,8 @@ abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
   ABX_CUDA_TRY(hist.alloc(4 * 256, s));
   ABX_CUDA_TRY(cudaMemsetAsync(hist.ptr, 0, 4 * 256 * sizeof(uint32_t), s));
   ABX_TRY(morton32_codes(s, kind, d_preds, nq, t->d_bounds, codes.ptr, hist.ptr));
-  ABX_TRY(radix_sort_u32(s, codes.ptr, perm.ptr, nullptr, nq, 4, hist.ptr));
+  ABX_TRY(radix_sort_u32(s, codes.ptr, perm.ptr, nullptr, nq, 4, hist.ptr,
+                         hybrid_top_passes(nq, 4)));
   return ABX_SUCCESS;
 }
 
@@ -994,7 +996,8 @@ abx_status abx_sort_u64(void *stream, uint64_t *d_keys, int64_t n, uint32_t *d_p
   if (n < 0 || (n > 0 && (!d_keys || !d_permutation)))
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_sort_u64: bad argument");
   device_state();
-  return radix_sort_u64(as_stream(stream), d_keys, d_permutation, nullptr, n, 8, nullptr);
+  return radix_sort_u64(as_stream(stream), d_keys, d_permutation, nullptr, n, 8, nullptr,
+                        hybrid_top_passes(n, 8));
 }
 
 abx_status abx_sort_u32(void *stream, uint32_t *d_keys, int64_t n, uint32_t *d_permutation)
@@ -1002,7 +1005,8 @@ abx_status abx_sort_u32(void *stream, uint32_t *d_keys, int64_t n, uint32_t *d_p
   if (n < 0 || (n > 0 && (!d_keys || !d_permutation)))
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_sort_u32: bad argument");
   device_state();
-  return radix_sort_u32(as_stream(stream), d_keys, d_permutation, nullptr, n, 4, nullptr);
+  return radix_sort_u32(as_stream(stream), d_keys, d_permutation, nullptr, n, 4, nullptr,
+                        hybrid_top_passes(n, 4));
 }
 
 abx_status abx_generate_hierarchy(void *stream, abx_geometry kind, const float *d_values,

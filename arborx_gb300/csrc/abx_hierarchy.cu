@@ -695,7 +695,8 @@ abx_status forest_build(cudaStream_t s, abx_geometry kind, const float *d_g, int
   }
   // stable by code over all trees, then stable by tree: a stable sort of
   // every tree by its own codes
-  ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, total, 8, hist.ptr));
+  ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, total, 8, hist.ptr,
+                         hybrid_top_passes(total, 8)));
   const uint32_t *final_perm = perm.ptr;
   int tree_bits = 0;
   while ((1ll << tree_bits) < nseg)

@@ -93,6 +93,7 @@ public:
   ~StageScope();
   StageScope(StageScope const &) = delete;
   StageScope &operator=(StageScope const &) = delete;
+  void add_kernels(int k) { kernels_ += k; }
 
 private:
   cudaStream_t stream_;
@@ -110,12 +111,23 @@ private:
 // otherwise d_hist holds num_passes x 256 counts (e.g. produced by the
 // Morton kernel).  When d_vals_in is null, the values start as 0..n-1.
 // On return the sorted keys and values are in d_keys / d_vals.
+//
+// top_passes > 0 (and < num_passes): only the top `top_passes` digits are
+// sorted by passes; a fix-up kernel then orders every run of equal top digits
+// (stable, exact), runs longer than kRunMax through a segmented sort of just
+// their elements.  Same result as the full sort, fewer passes over memory
+// when the top digits already spread the keys (Morton codes of n points with
+// n << 2^(8 top_passes)).  This variant synchronises the stream once.
 abx_status radix_sort_u64(cudaStream_t s, uint64_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,
-                          const uint32_t *d_hist);
+                          const uint32_t *d_hist, int top_passes = 0);
 abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,
-                          const uint32_t *d_hist);
+                          const uint32_t *d_hist, int top_passes = 0);
+
+// Number of top passes of the hybrid sort for n keys of num_passes digits
+// (0 = plain LSD).
+int hybrid_top_passes(int64_t n, int num_passes);
 
 // Exclusive scan of n int32 into n + 1 outputs; *d_total_out (optional,
 // device int64) receives the 64-bit total.  Raises ABX_DEVERR_BAD_INPUT when

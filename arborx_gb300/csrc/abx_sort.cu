@@ -298,17 +298,124 @@ __global__ void __launch_bounds__(kSortThreads, 3)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Run fix-up of the hybrid sort
+// ---------------------------------------------------------------------------
+
+constexpr int kRunMax = 32;
+
+// Bounds [a, b) of the run of equal top bits (key >> shift) around i, the
+// scan stopping once the run is known to exceed kRunMax.
 template <class K>
-abx_status radix_sort_impl(cudaStream_t s, K *d_keys, uint32_t *d_vals,
-                           const uint32_t *d_vals_in, int64_t n, int num_passes,
-                           const uint32_t *d_hist)
+__device__ __forceinline__ void run_bounds(const K *__restrict__ keys, int64_t n, int64_t i,
+                                           K top, int shift, int64_t &a, int64_t &b)
 {
-  if (n <= 0)
-    return ABX_SUCCESS;
-  if (n > (int64_t)INT32_MAX)
-    return fail(ABX_ERROR_INVALID_ARGUMENT, "radix sort: more than 2^31-1 keys");
-  if (num_passes < 1 || num_passes > (int)(sizeof(K) * 8 / 8))
-    return fail(ABX_ERROR_INVALID_ARGUMENT, "radix sort: bad number of passes");
+  a = i;
+  while (a > 0 && i - a <= kRunMax && (keys[a - 1] >> shift) == top)
+    --a;
+  b = i + 1;
+  while (b < n && b - a <= kRunMax && (keys[b] >> shift) == top)
+    ++b;
+}
+
+// Keys sorted (stably) by their top bits: place every key of a run of at
+// most kRunMax equal top-bit keys at its rank by (key, position), which is the
+// stable order; keys of longer runs are copied in place and counted.
+template <class K>
+__global__ void __launch_bounds__(256)
+    k_run_fixup(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
+                uint32_t *__restrict__ vout, int64_t n, int shift,
+                unsigned long long *__restrict__ long_count)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool is_long = false;
+  if (i < n)
+  {
+    const K k = kin[i];
+    int64_t a, b;
+    run_bounds(kin, n, i, (K)(k >> shift), shift, a, b);
+    int64_t r = i;
+    if (b - a > kRunMax)
+      is_long = true;
+    else
+    {
+      r = a;
+      for (int64_t j = a; j < b; ++j)
+      {
+        const K kj = kin[j];
+        r += (kj < k) || (kj == k && j < i);
+      }
+    }
+    kout[r] = k;
+    vout[r] = vin[i];
+  }
+  const unsigned ballot = __ballot_sync(0xffffffffu, is_long);
+  if (ballot && (threadIdx.x & 31) == (unsigned)(__ffs(ballot) - 1))
+    atomicAdd(long_count, (unsigned long long)__popc(ballot));
+}
+
+// Flags of the keys in long runs, and of the first key of each long run.
+template <class K>
+__global__ void __launch_bounds__(256)
+    k_long_flags(const K *__restrict__ kin, int64_t n, int shift, int32_t *__restrict__ is_long,
+                 int32_t *__restrict__ is_start)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  const K top = kin[i] >> shift;
+  int64_t a, b;
+  run_bounds(kin, n, i, top, shift, a, b);
+  const bool lg = b - a > kRunMax;
+  is_long[i] = lg;
+  is_start[i] = lg && (i == 0 || (kin[i - 1] >> shift) != top);
+}
+
+// Compact the long-run keys: composite key (run index above the low bits)
+// and their positions.
+template <class K>
+__global__ void __launch_bounds__(256)
+    k_long_compact(const K *__restrict__ kin, int64_t n, int shift,
+                   const int32_t *__restrict__ is_long, const int32_t *__restrict__ long_pos,
+                   const int32_t *__restrict__ is_start, const int32_t *__restrict__ run_excl,
+                   K *__restrict__ ckeys, uint32_t *__restrict__ cpos)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !is_long[i])
+    return;
+  const int64_t c = long_pos[i];
+  const K run = (K)(run_excl[i] + is_start[i] - 1);
+  const K low = kin[i] & (((K)1 << shift) - 1);
+  ckeys[c] = (run << shift) | low;
+  cpos[c] = (uint32_t)i;
+}
+
+// Position c of the long-run list receives the key ranked c-th.
+template <class K>
+__global__ void __launch_bounds__(256)
+    k_long_gather(const K *__restrict__ kin, const uint32_t *__restrict__ vin,
+                  K *__restrict__ kout, uint32_t *__restrict__ vout,
+                  const uint32_t *__restrict__ cpos, const uint32_t *__restrict__ cperm, int64_t m)
+{
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= m)
+    return;
+  const uint32_t src = cpos[cperm[c]];
+  const uint32_t dst = cpos[c];
+  kout[dst] = kin[src];
+  vout[dst] = vin[src];
+}
+
+// The passes of digits [first, num_passes) (LSD order), from (d_keys,
+// d_vals_in or the identity) to *kin_out / *vin_out, which are d_keys / d_vals
+// or the alternate buffers.  Returns the number of kernels launched in
+// *launches.
+template <class K>
+abx_status sort_passes(cudaStream_t s, K *d_keys, uint32_t *d_vals, const uint32_t *d_vals_in,
+                       int64_t n, int first, int num_passes, const uint32_t *d_hist,
+                       K *keys_alt, uint32_t *vals_alt, const K **kin_out,
+                       const uint32_t **vin_out, int &launches)
+{
   DeviceState &ds = device_state();
   const int64_t num_tiles = (n + kTile - 1) / kTile;
 
@@ -324,20 +431,16 @@ abx_status radix_sort_impl(cudaStream_t s, K *d_keys, uint32_t *d_vals,
   unsigned long long *lookback = reinterpret_cast<unsigned long long *>(work.ptr + head_bytes);
   ABX_CUDA_TRY(cudaMemsetAsync(work.ptr, 0, head_bytes + lookback_words * 8, s));
 
-  Scratch<K> keys_alt;
-  Scratch<uint32_t> vals_alt;
-  ABX_CUDA_TRY(keys_alt.alloc(n, s));
-  ABX_CUDA_TRY(vals_alt.alloc(n, s));
-
-  StageScope scope(s, sizeof(K) == 8 ? "sort64" : "sort32", num_passes + (d_hist ? 1 : 2));
   const uint32_t *hsrc = d_hist;
   if (!hsrc)
   {
     int blocks = (int)std::min<int64_t>((n + 255) / 256, (int64_t)ds.num_sms * 8);
     k_histogram<K><<<blocks, 256, 0, s>>>(d_keys, n, num_passes, hist);
     hsrc = hist;
+    ++launches;
   }
   k_hist_scan<<<num_passes, kBins, 0, s>>>(hsrc, offsets);
+  ++launches;
 
   const size_t smem = sizeof(PassSmem<K>);
   static bool attr_set = false;
@@ -350,26 +453,141 @@ abx_status radix_sort_impl(cudaStream_t s, K *d_keys, uint32_t *d_vals,
 
   const K *kin = d_keys;
   const uint32_t *vin = d_vals_in;
-  K *kout = keys_alt.ptr;
-  uint32_t *vout = vals_alt.ptr;
-  for (int p = 0; p < num_passes; ++p)
+  K *kout = keys_alt;
+  uint32_t *vout = vals_alt;
+  for (int p = first; p < num_passes; ++p)
   {
     k_onesweep<K><<<(unsigned)num_tiles, kSortThreads, smem, s>>>(
         kin, vin, kout, vout, n, 8 * p, p, offsets + p * kBins, lookback, counters + p,
         ds.d_error);
     ABX_CUDA_TRY(cudaGetLastError());
+    ++launches;
     const K *nk = kout;
     const uint32_t *nv = vout;
-    kout = (kout == keys_alt.ptr) ? d_keys : keys_alt.ptr;
-    vout = (vout == vals_alt.ptr) ? d_vals : vals_alt.ptr;
+    kout = (kout == keys_alt) ? d_keys : keys_alt;
+    vout = (vout == vals_alt) ? d_vals : vals_alt;
     kin = nk;
     vin = nv;
   }
+  *kin_out = kin;
+  *vin_out = vin;
+  return ABX_SUCCESS;
+}
+
+template <class K>
+abx_status radix_sort_full(cudaStream_t s, K *d_keys, uint32_t *d_vals,
+                           const uint32_t *d_vals_in, int64_t n, int num_passes,
+                           const uint32_t *d_hist, int &launches)
+{
+  Scratch<K> keys_alt;
+  Scratch<uint32_t> vals_alt;
+  ABX_CUDA_TRY(keys_alt.alloc(n, s));
+  ABX_CUDA_TRY(vals_alt.alloc(n, s));
+  const K *kin;
+  const uint32_t *vin;
+  ABX_TRY(sort_passes<K>(s, d_keys, d_vals, d_vals_in, n, 0, num_passes, d_hist, keys_alt.ptr,
+                         vals_alt.ptr, &kin, &vin, launches));
   if (kin != d_keys)
     ABX_CUDA_TRY(cudaMemcpyAsync(d_keys, kin, n * sizeof(K), cudaMemcpyDeviceToDevice, s));
   if (vin != d_vals)
     ABX_CUDA_TRY(cudaMemcpyAsync(d_vals, vin, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
   return ABX_SUCCESS;
+}
+
+// Top passes, run fix-up, long runs through a segmented sort of their keys.
+template <class K>
+abx_status radix_sort_hybrid(cudaStream_t s, K *d_keys, uint32_t *d_vals,
+                             const uint32_t *d_vals_in, int64_t n, int num_passes,
+                             const uint32_t *d_hist, int top, int &launches)
+{
+  const int first = num_passes - top;
+  const int shift = 8 * first;
+  Scratch<K> keys_alt;
+  Scratch<uint32_t> vals_alt;
+  ABX_CUDA_TRY(keys_alt.alloc(n, s));
+  ABX_CUDA_TRY(vals_alt.alloc(n, s));
+  const K *kin;
+  const uint32_t *vin;
+  ABX_TRY(sort_passes<K>(s, d_keys, d_vals, d_vals_in, n, first, num_passes, d_hist,
+                         keys_alt.ptr, vals_alt.ptr, &kin, &vin, launches));
+  // the fix-up is out of place: into d_keys / d_vals, or through the
+  // alternate buffers when the passes ended in d_keys
+  const bool via_alt = kin == d_keys;
+  K *kout = via_alt ? keys_alt.ptr : d_keys;
+  uint32_t *vout = via_alt ? vals_alt.ptr : d_vals;
+  Scratch<unsigned long long> long_count;
+  ABX_CUDA_TRY(long_count.alloc(1, s));
+  ABX_CUDA_TRY(cudaMemsetAsync(long_count.ptr, 0, sizeof(unsigned long long), s));
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  k_run_fixup<K><<<blocks, 256, 0, s>>>(kin, vin, kout, vout, n, shift, long_count.ptr);
+  ABX_CUDA_TRY(cudaGetLastError());
+  ++launches;
+  unsigned long long m = 0;
+  ABX_CUDA_TRY(cudaMemcpyAsync(&m, long_count.ptr, sizeof(m), cudaMemcpyDeviceToHost, s));
+  ABX_CUDA_TRY(cudaStreamSynchronize(s));
+  if (m > 0)
+  {
+    // runs have more than kRunMax keys: fewer than n / (kRunMax + 1) of them
+    const int64_t max_runs = (int64_t)m / (kRunMax + 1) + 1;
+    int run_bits = 0;
+    while ((1ll << run_bits) < max_runs)
+      ++run_bits;
+    if (shift + run_bits > (int)(8 * sizeof(K)))
+      return fail(ABX_ERROR_NOT_SUPPORTED, "radix sort: too many long runs");
+    Scratch<int32_t> is_long, is_start, long_pos, run_excl;
+    ABX_CUDA_TRY(is_long.alloc(n, s));
+    ABX_CUDA_TRY(is_start.alloc(n, s));
+    ABX_CUDA_TRY(long_pos.alloc(n + 1, s));
+    ABX_CUDA_TRY(run_excl.alloc(n + 1, s));
+    k_long_flags<K><<<blocks, 256, 0, s>>>(kin, n, shift, is_long.ptr, is_start.ptr);
+    ABX_CUDA_TRY(cudaGetLastError());
+    ABX_TRY(exclusive_scan_i32(s, is_long.ptr, n, long_pos.ptr));
+    ABX_TRY(exclusive_scan_i32(s, is_start.ptr, n, run_excl.ptr));
+    Scratch<K> ckeys;
+    Scratch<uint32_t> cpos, cperm;
+    ABX_CUDA_TRY(ckeys.alloc(m, s));
+    ABX_CUDA_TRY(cpos.alloc(m, s));
+    ABX_CUDA_TRY(cperm.alloc(m, s));
+    k_long_compact<K><<<blocks, 256, 0, s>>>(kin, n, shift, is_long.ptr, long_pos.ptr,
+                                              is_start.ptr, run_excl.ptr, ckeys.ptr, cpos.ptr);
+    ABX_CUDA_TRY(cudaGetLastError());
+    launches += 3 + 2 * 3; // flags, compact, gather; two scans of 3 kernels
+    ABX_TRY(radix_sort_full<K>(s, ckeys.ptr, cperm.ptr, nullptr, (int64_t)m,
+                               (shift + run_bits + 7) / 8, nullptr, launches));
+    k_long_gather<K><<<(unsigned)((m + 255) / 256), 256, 0, s>>>(kin, vin, kout, vout, cpos.ptr,
+                                                                cperm.ptr, (int64_t)m);
+    ABX_CUDA_TRY(cudaGetLastError());
+  }
+  if (via_alt)
+  {
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_keys, kout, n * sizeof(K), cudaMemcpyDeviceToDevice, s));
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_vals, vout, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  }
+  return ABX_SUCCESS;
+}
+
+template <class K>
+abx_status radix_sort_impl(cudaStream_t s, K *d_keys, uint32_t *d_vals,
+                           const uint32_t *d_vals_in, int64_t n, int num_passes,
+                           const uint32_t *d_hist, int top)
+{
+  if (n <= 0)
+    return ABX_SUCCESS;
+  if (n > (int64_t)INT32_MAX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "radix sort: more than 2^31-1 keys");
+  if (num_passes < 1 || num_passes > (int)(sizeof(K) * 8 / 8))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "radix sort: bad number of passes");
+  if (top < 0 || top >= num_passes)
+    top = 0;
+  StageScope scope(s, sizeof(K) == 8 ? "sort64" : "sort32", 0);
+  int launches = 0;
+  abx_status st = top > 0
+                      ? radix_sort_hybrid<K>(s, d_keys, d_vals, d_vals_in, n, num_passes, d_hist,
+                                             top, launches)
+                      : radix_sort_full<K>(s, d_keys, d_vals, d_vals_in, n, num_passes, d_hist,
+                                           launches);
+  scope.add_kernels(launches);
+  return st;
 }
 
 // ---------------------------------------------------------------------------
@@ -501,16 +719,27 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int32_t *__re
 
 abx_status radix_sort_u64(cudaStream_t s, uint64_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,
-                          const uint32_t *d_hist)
+                          const uint32_t *d_hist, int top_passes)
 {
-  return radix_sort_impl<uint64_t>(s, d_keys, d_vals, d_vals_in, n, num_passes, d_hist);
+  return radix_sort_impl<uint64_t>(s, d_keys, d_vals, d_vals_in, n, num_passes, d_hist,
+                                   top_passes);
 }
 
 abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,
-                          const uint32_t *d_hist)
+                          const uint32_t *d_hist, int top_passes)
 {
-  return radix_sort_impl<uint32_t>(s, d_keys, d_vals, d_vals_in, n, num_passes, d_hist);
+  return radix_sort_impl<uint32_t>(s, d_keys, d_vals, d_vals_in, n, num_passes, d_hist,
+                                   top_passes);
+}
+
+int hybrid_top_passes(int64_t n, int num_passes)
+{
+  // 3 top digits (24 bits) spread up to ~2^24 keys into short runs; below
+  // 2^16 keys the plain sort is as cheap
+  if (n < (1 << 16) || num_passes <= 3)
+    return 0;
+  return tuning_value("SORT_TOP_PASSES", 3);
 }
 
 abx_status exclusive_scan_i32(cudaStream_t s, const int32_t *d_in, int64_t n, int32_t *d_out)

@@ -58,7 +58,9 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1_000_000,
                     help="queries timed per CPU step (scaled to --nq)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--case", default="knn", choices=["knn", "build", "nearest", "radius"],
+    ap.add_argument("--clouds", type=int, default=4096,
+                    help="--case forest: number of point clouds (trees)")
+    ap.add_argument("--case", default="knn", choices=["knn", "build", "nearest", "radius", "forest"],
                     help="knn: the benchmark step (build + kNN); build / nearest / radius: "
                     "one stage alone (profiling cases; radius = 2-pass CRS search with "
                     "~32 expected neighbours)")
@@ -535,10 +537,98 @@ def run_case(args):
     }), flush=True)
 
 
+def make_clouds(ncl):
+    """The batched workload: ncl clouds of floor(10^U(2,5)) points (seed 13);
+    cloud i has its lower corner in U[0,100)^3 and extents 10^U(-1,1) per axis
+    (seed 14), its points uniform in that box (seed 15 + i).  One query per
+    point: the box centred on it with full edge 0.02 x its cloud's extent."""
+    sizes = np.floor(10.0 ** np.random.default_rng(13).uniform(2, 5, ncl)).astype(np.int64)
+    rng = np.random.default_rng(14)
+    corner = rng.uniform(0, 100, (ncl, 3)).astype(np.float32)
+    extent = (10.0 ** rng.uniform(-1, 1, (ncl, 3))).astype(np.float32)
+    offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    pts = np.empty((int(offsets[-1]), 3), np.float32)
+    boxes = np.empty((int(offsets[-1]), 6), np.float32)
+    for i in range(ncl):
+        a, b = offsets[i], offsets[i + 1]
+        p = corner[i] + extent[i] * np.random.default_rng(15 + i).random((b - a, 3), dtype=np.float32)
+        pts[a:b] = p
+        half = np.float32(0.01) * extent[i]
+        boxes[a:b, :3] = p - half
+        boxes[a:b, 3:] = p + half
+    return pts, boxes, offsets
+
+
+def run_forest(args):
+    """Batched vs plain on the many-clouds workload: one Forest build + one
+    forest box query, against the per-tree loop (one BVH build and one query
+    per cloud on one stream, the reference's many-trees pattern,
+    benchmarks/execution_space_instances/execution_space_instances_driver.cpp:
+    187-233).  Both arms time on the host clock around a device sync (the
+    plain loop's cost is largely per-call), and their CRS outputs are
+    compared for equality."""
+    import torch
+
+    import arborx_gb300 as ax
+    from arborx_gb300 import build as libbuild
+
+    libbuild.build()
+    pts_np, boxes_np, off = make_clouds(args.clouds)
+    pts = torch.from_numpy(pts_np).cuda()
+    boxes = torch.from_numpy(boxes_np).cuda()
+    ntrees = off.size - 1
+    views = [(pts[off[t]:off[t + 1]], boxes[off[t]:off[t + 1]]) for t in range(ntrees)]
+
+    def batched():
+        f = ax.Forest(pts, off)
+        return f.query(ax.intersects(boxes), off)
+
+    def plain():
+        out = []
+        for p, b in views:
+            out.append(ax.query(ax.BoundingVolumeHierarchy(p), ax.intersects(b)))
+        return out
+
+    def timed(fn, steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            r = fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / steps, r
+
+    for _ in range(args.warmup):
+        batched()
+    tb, (bi, bo) = timed(batched, args.steps)
+    plain()
+    tp, per = timed(plain, max(1, min(args.steps, 3)))
+    bo_h = bo.cpu().numpy()
+    bi_h = bi.cpu().numpy()
+    same = True
+    for t, (i, o) in enumerate(per):
+        seg = bo_h[off[t]:off[t + 1] + 1]
+        if not (np.array_equal(seg - seg[0], o.cpu().numpy())
+                and np.array_equal(bi_h[seg[0]:seg[-1]], i.cpu().numpy())):
+            same = False
+            break
+    total = int(off[-1])
+    print(json.dumps({
+        "case": "forest", "clouds": ntrees, "points": total, "queries": total,
+        "results": int(bo_h[-1]),
+        "batched_ms": tb * 1e3, "plain_ms": tp * 1e3, "speedup": tp / tb,
+        "batched_points_per_s": total / tb, "plain_points_per_s": total / tp,
+        "bit_exact": same,
+    }), flush=True)
+    if not same:
+        sys.exit(1)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.case == "forest":
+        run_forest(args)
     elif args.case != "knn":
         run_case(args)
     else:

@@ -163,3 +163,48 @@ def test_build_is_deterministic(ax):
         again = [x.cpu().numpy() for x in ax.BoundingVolumeHierarchy(t).export_nodes()]
         assert all(np.array_equal(a, b) for a, b in zip(first, again))
     assert ax.device_errors() == 0
+
+
+def _hybrid_cases(n, seed):
+    rng = np.random.default_rng(seed)
+    uniform = rng.integers(0, 1 << 63, size=n, dtype=np.uint64)
+    # clustered: few distinct top digits, random low bits (long runs)
+    clustered = (rng.integers(0, 50, n, dtype=np.uint64) << np.uint64(40)) | rng.integers(
+        0, 1 << 20, n, dtype=np.uint64)
+    same_top = np.uint64(7 << 50) | rng.integers(0, 8, n, dtype=np.uint64)
+    equal = np.full(n, 12345, np.uint64)
+    mixed = uniform.copy()
+    mixed[: n // 3] = clustered[: n // 3]
+    return [uniform, clustered, same_top, equal, mixed]
+
+
+@pytest.mark.parametrize("top", ["0", "3"])
+def test_sort_u64_hybrid_top_passes(ax, top):
+    """The top-digit passes + run fix-up (+ long-run segmented sort) give the
+    full stable sort on uniform, clustered, one-run and all-equal keys."""
+    from arborx_gb300 import _lib
+
+    L = _lib.load()
+    L.abx_tuning_set(b"SORT_TOP_PASSES", int(top))
+    try:
+        for keys in _hybrid_cases(300007, 5):
+            t = cuda(keys.view(np.int64))
+            perm = ax.sort_u64(t).cpu().numpy().view(np.uint32)
+            ref = np.argsort(keys, kind="stable")
+            assert np.array_equal(perm, ref.astype(np.uint32))
+            assert np.array_equal(t.cpu().numpy().view(np.uint64), keys[ref])
+    finally:
+        L.abx_tuning_reset()
+    assert ax.device_errors() == 0
+
+
+def test_sort_u32_hybrid(ax):
+    rng = np.random.default_rng(6)
+    n = 500009
+    for keys in (rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32),
+                 (rng.integers(0, 3, n, dtype=np.uint32) << np.uint32(8)) | rng.integers(0, 256, n, dtype=np.uint32)):
+        t = cuda(keys.view(np.int32))
+        perm = ax.sort_u32(t).cpu().numpy().view(np.uint32)
+        ref = np.argsort(keys, kind="stable").astype(np.uint32)
+        assert np.array_equal(perm, ref)
+        assert np.array_equal(t.cpu().numpy().view(np.uint32), keys[ref])
