@@ -222,8 +222,11 @@ __global__ void k_single_leaf(const float *__restrict__ g, LeafNode *__restrict_
                               float *__restrict__ bounds)
 {
   Box3 b = load_leaf_box<KIND>(g, 0);
-  leaves[0].rope = kRopeSentinel;
-  leaves[0].value = 0;
+  if (leaves)
+  {
+    leaves[0].rope = kRopeSentinel;
+    leaves[0].value = 0;
+  }
   SortedLeaf<KIND>::store(sorted, 0, b, 0);
   tnodes[0] = make_tnode(b, bucket_ref(0), 1, empty_box(), bucket_ref(0), 0); // leaf value 0
 #pragma unroll

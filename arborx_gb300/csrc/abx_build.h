@@ -33,15 +33,22 @@ abx_status generate_hierarchy(cudaStream_t s, abx_geometry kind, const float *d_
 abx_status generate_hierarchy_segments(cudaStream_t s, abx_geometry kind, const float *d_g,
                                        int64_t total, const int64_t *d_off, int nseg,
                                        const uint32_t *d_perm, const uint64_t *d_codes,
-                                       LeafNode *d_leaves, InternalNode *d_internal,
                                        TNode *d_tnodes, float4 *d_sorted);
+
+// The reference-layout arrays (leaves {rope, value}, internal nodes
+// {left_child, rope, box}; ArborX_Node.hpp:24-51) of the tree whose sorted
+// positions and node slots start at lo, derived from its child-pair nodes
+// and Morton-ordered leaves.  Either output may be null.
+abx_status export_reference_layout(cudaStream_t s, abx_geometry kind, const TNode *d_tnodes,
+                                   const float4 *d_sorted, int64_t lo, int64_t n,
+                                   LeafNode *d_leaves, InternalNode *d_internal);
 
 // Batched build of nseg trees given as segments of d_g (d_off on the device):
 // per-tree bounds (d_bounds, 6 floats per tree), per-tree Morton codes, a
 // stable sort of every tree, the segmented hierarchy.
 abx_status forest_build(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t total,
-                        const int64_t *d_off, int nseg, float *d_bounds, LeafNode *d_leaves,
-                        InternalNode *d_internal, TNode *d_tnodes, float4 *d_sorted);
+                        const int64_t *d_off, int nseg, float *d_bounds, TNode *d_tnodes,
+                        float4 *d_sorted);
 
 // Query order of a forest batch: by tree, then Morton32 within the tree's box.
 abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const float *d_preds,
@@ -52,7 +59,7 @@ abx_status single_leaf(cudaStream_t s, abx_geometry kind, const float *d_g,
                        LeafNode *d_leaves, TNode *d_tnodes, float4 *d_sorted, float *d_bounds);
 
 // Leaves per CTA of the block-local hierarchy climb.
-constexpr int kHierBlock = 512;
+constexpr int kHierBlock = 256;
 
 // Largest subtree whose leaves a query may scan as one bucket, the flag of a
 // child slot's count field marking "Karras index = right end of the range",

@@ -23,9 +23,7 @@ struct abx_bvh
   cudaStream_t stream = nullptr;
   abx_geometry kind = ABX_POINT;
   int64_t n = 0;
-  abx::LeafNode *leaves = nullptr;
-  abx::InternalNode *internal = nullptr;
-  abx::TNode *tnodes = nullptr;
+  abx::TNode *tnodes = nullptr; // child-pair nodes, one slot per Karras index
   float4 *sorted = nullptr;  // leaf geometry in Morton order (bucket scans)
   float *d_bounds = nullptr; // tree bounds on the device (6 floats per tree)
   float *h_bounds = nullptr; // pinned copy, valid once `ready` completed
@@ -210,8 +208,6 @@ void destroy_tree(abx_bvh *t)
   if (!t)
     return;
   cudaStream_t s = t->stream;
-  dfree(t->leaves, s);
-  dfree(t->internal, s);
   dfree(t->tnodes, s);
   dfree(t->sorted, s);
   dfree(t->d_bounds, s);
@@ -251,17 +247,15 @@ abx_status build_tree(abx_bvh *t, const float *d_values)
     ABX_CUDA_TRY(cudaStreamSynchronize(s));
     return ABX_SUCCESS;
   }
-  ABX_CUDA_TRY(dmalloc_n(&t->leaves, n, s));
   const int f4 = t->kind == ABX_BOX ? 2 : 1;
   ABX_CUDA_TRY(dmalloc_n(&t->sorted, (size_t)n * f4, s));
   if (n == 1)
   {
     ABX_CUDA_TRY(dmalloc_n(&t->tnodes, 1, s));
-    ABX_TRY(single_leaf(s, t->kind, d_values, t->leaves, t->tnodes, t->sorted, t->d_bounds));
+    ABX_TRY(single_leaf(s, t->kind, d_values, nullptr, t->tnodes, t->sorted, t->d_bounds));
   }
   else
   {
-    ABX_CUDA_TRY(dmalloc_n(&t->internal, n - 1, s));
     ABX_CUDA_TRY(dmalloc_n(&t->tnodes, n - 1, s));
     Scratch<uint64_t> codes;
     Scratch<uint32_t> perm;
@@ -276,8 +270,8 @@ abx_status build_tree(abx_bvh *t, const float *d_values)
     ABX_TRY(morton64_codes(s, t->kind, d_values, n, t->d_bounds, codes.ptr, hist.ptr));
     ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, n, 8, hist.ptr,
                            hybrid_top_passes(n, 8)));
-    ABX_TRY(generate_hierarchy(s, t->kind, d_values, n, perm.ptr, codes.ptr, t->leaves,
-                               t->internal, t->tnodes, t->sorted));
+    ABX_TRY(generate_hierarchy(s, t->kind, d_values, n, perm.ptr, codes.ptr, nullptr, nullptr,
+                               t->tnodes, t->sorted));
   }
   ABX_CUDA_TRY(cudaMemcpyAsync(t->h_bounds, t->d_bounds, 6 * sizeof(float),
                                cudaMemcpyDeviceToHost, s));
@@ -299,13 +293,11 @@ abx_status build_forest(abx_bvh *t, const float *d_values)
   if (total > 0)
   {
     const int f4 = t->kind == ABX_BOX ? 2 : 1;
-    ABX_CUDA_TRY(dmalloc_n(&t->leaves, total, s));
-    ABX_CUDA_TRY(dmalloc_n(&t->internal, total, s));
     ABX_CUDA_TRY(dmalloc_n(&t->tnodes, total, s));
     ABX_CUDA_TRY(dmalloc_n(&t->sorted, (size_t)total * f4, s));
   }
-  ABX_TRY(forest_build(s, t->kind, d_values, total, t->d_off, nt, t->d_bounds, t->leaves,
-                       t->internal, t->tnodes, t->sorted));
+  ABX_TRY(forest_build(s, t->kind, d_values, total, t->d_off, nt, t->d_bounds, t->tnodes,
+                       t->sorted));
   ABX_CUDA_TRY(cudaMemcpyAsync(t->h_bounds, t->d_bounds, (size_t)6 * nt * sizeof(float),
                                cudaMemcpyDeviceToHost, s));
   return ABX_SUCCESS;
@@ -741,13 +733,12 @@ abx_status abx_bvh_export_nodes(const abx_bvh *bvh, void *stream, int32_t *d_lea
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_export_nodes: null tree");
   cudaStream_t s = as_stream(stream);
   ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
-  if (d_leaves && bvh->n > 0)
-    ABX_CUDA_TRY(cudaMemcpyAsync(d_leaves, bvh->leaves, bvh->n * sizeof(LeafNode),
-                                 cudaMemcpyDeviceToDevice, s));
-  if (d_internal && bvh->n > 1)
-    ABX_CUDA_TRY(cudaMemcpyAsync(d_internal, bvh->internal, (bvh->n - 1) * sizeof(InternalNode),
-                                 cudaMemcpyDeviceToDevice, s));
-  return ABX_SUCCESS;
+  if (!d_leaves && !d_internal)
+    return ABX_SUCCESS;
+  device_state();
+  return export_reference_layout(s, bvh->kind, bvh->tnodes, bvh->sorted, 0, bvh->n,
+                                 reinterpret_cast<LeafNode *>(d_leaves),
+                                 reinterpret_cast<InternalNode *>(d_internal));
 }
 
 abx_status abx_bvh_device_view(const abx_bvh *bvh, abx_device_view *out)
@@ -893,13 +884,12 @@ abx_status abx_forest_export_nodes(const abx_forest *forest, int32_t tree, void 
   ABX_CUDA_TRY(cudaStreamWaitEvent(s, forest->ready, 0));
   const int64_t lo = forest->h_off[tree];
   const int64_t n = forest->h_off[tree + 1] - lo;
-  if (d_leaves && n > 0)
-    ABX_CUDA_TRY(cudaMemcpyAsync(d_leaves, forest->leaves + lo, n * sizeof(LeafNode),
-                                 cudaMemcpyDeviceToDevice, s));
-  if (d_internal && n > 1)
-    ABX_CUDA_TRY(cudaMemcpyAsync(d_internal, forest->internal + lo,
-                                 (n - 1) * sizeof(InternalNode), cudaMemcpyDeviceToDevice, s));
-  return ABX_SUCCESS;
+  if (!d_leaves && !d_internal)
+    return ABX_SUCCESS;
+  device_state();
+  return export_reference_layout(s, forest->kind, forest->tnodes, forest->sorted, lo, n,
+                                 reinterpret_cast<LeafNode *>(d_leaves),
+                                 reinterpret_cast<InternalNode *>(d_internal));
 }
 
 namespace

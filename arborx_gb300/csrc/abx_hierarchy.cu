@@ -62,19 +62,19 @@ __device__ __forceinline__ int child_count_field(int kidx, int lo, int hi)
   return c | (kidx == hi ? kBucketRightEnd : 0);
 }
 
-__device__ __forceinline__ Box3 load_internal_box_cg(const InternalNode *node)
+// Box of an internal node written by another CTA: the union of the two
+// child boxes of its child-pair node, read through L2.
+__device__ __forceinline__ Box3 load_tnode_box_cg(const TNode *node)
 {
-  const float *f = reinterpret_cast<const float *>(node);
-  const float2 a = __ldcg(reinterpret_cast<const float2 *>(f + 2));
-  const float4 b = __ldcg(reinterpret_cast<const float4 *>(f + 4));
-  Box3 r;
-  r.lo[0] = a.x;
-  r.lo[1] = a.y;
-  r.lo[2] = b.x;
-  r.hi[0] = b.y;
-  r.hi[1] = b.z;
-  r.hi[2] = b.w;
-  return r;
+  const float4 *f = reinterpret_cast<const float4 *>(node);
+  TNode t;
+  t.a = __ldcg(f);
+  t.b = __ldcg(f + 1);
+  t.c = __ldcg(f + 2);
+  Box3 l, r;
+  tnode_children(t, l, r);
+  expand(l, r);
+  return l;
 }
 
 // State of a climb that leaves its CTA (handed from k_hierarchy_local to
@@ -83,62 +83,40 @@ struct __align__(16) ClimbState
 {
   int range_left, range_right; // global positions
   int cur_node;                // global slot of the node completed last, -1 for a leaf
-  int node_num;                // its tree-local node number
   int value;                   // leaf value when cur_node == -1
   int lo, hi;                  // the tree's positions
-  int pad;
+  int pad[2];
   float blo[3];
   float bhi[3];
   float pad2[2];
 };
 static_assert(sizeof(ClimbState) == 64, "climb state is 64 B");
 
-// The parent created by a climb step.  Writes its 64-byte child-pair node and
-// its reference-layout record; returns its box in `box`.
-struct ParentStep
+// Child-pair node of the parent with Karras index kp; `box` (the climbing
+// child's) becomes the parent's box.
+__device__ __forceinline__ void write_parent(TNode *__restrict__ tnodes, int kp,
+                                             bool is_left_child, Box3 &box, int own_ref,
+                                             int own_c, Box3 const &sib, int sib_ref, int sib_c)
 {
-  int kp;         // Karras index of the parent (global slot)
-  int left_child; // tree-local node number of its left child
-  int rope;       // tree-local rope
-};
-
-__device__ __forceinline__ void write_parent(TNode *__restrict__ tnodes,
-                                             InternalNode *__restrict__ internal,
-                                             ParentStep const &ps, bool is_left_child, Box3 &box,
-                                             int own_ref, int own_c, Box3 const &sib, int sib_ref,
-                                             int sib_c)
-{
-  tnodes[ps.kp] = is_left_child ? make_tnode(box, own_ref, own_c, sib, sib_ref, sib_c)
-                                : make_tnode(sib, sib_ref, sib_c, box, own_ref, own_c);
+  tnodes[kp] = is_left_child ? make_tnode(box, own_ref, own_c, sib, sib_ref, sib_c)
+                             : make_tnode(sib, sib_ref, sib_c, box, own_ref, own_c);
   expand(box, sib);
-  InternalNode node;
-  node.left_child = ps.left_child;
-  node.rope = ps.rope;
-#pragma unroll
-  for (int d = 0; d < 3; ++d)
-  {
-    node.lo[d] = box.lo[d];
-    node.hi[d] = box.hi[d];
-  }
-  internal[ps.kp] = node;
 }
 
 // Apetrei's climb with global flags (ArborX_TreeConstruction.hpp:197-311):
-// relaxed compare-and-swap on the parent's range slot; a release fence before
-// it once this thread has written a node record in this kernel (`wrote`;
-// records written by an earlier kernel are already visible); an acquire
-// fence before reading an internal sibling's box through L2.  The first
-// arriver at a parent stops; nothing spins.  Stops at the tree's root.
+// relaxed compare-and-swap on the parent's range slot, preceded by a release
+// fence once this thread's node may have been written in this kernel
+// (`wrote`); an acquire fence before reading an internal sibling's node
+// through L2.  The first arriver at a parent stops; nothing spins.  Stops at
+// the tree's root.
 template <int KIND>
 __device__ void climb_global(const float *__restrict__ g, const uint32_t *__restrict__ perm,
                              const uint64_t *__restrict__ codes, int *__restrict__ ranges,
-                             InternalNode *__restrict__ internal, TNode *__restrict__ tnodes,
-                             ClimbState st, bool wrote)
+                             TNode *__restrict__ tnodes, ClimbState st, bool wrote)
 {
   const int lo = st.lo, hi = st.hi;
-  const int num_internal = hi - lo; // tree-local
   int range_left = st.range_left, range_right = st.range_right;
-  int cur_node = st.cur_node, node_num = st.node_num;
+  int cur_node = st.cur_node;
   Box3 box;
 #pragma unroll
   for (int d = 0; d < 3; ++d)
@@ -154,16 +132,14 @@ __device__ void climb_global(const float *__restrict__ g, const uint32_t *__rest
     const int p = is_left_child ? range_right : range_left - 1;
     const int own_lo = range_left, own_hi = range_right;
     if (wrote)
-      fence_acq_rel_gpu(); // release internal[cur_node]
+      fence_acq_rel_gpu(); // release tnodes[cur_node]
     const int old = atomic_cas_relaxed(ranges + p, -1, is_left_child ? range_left : range_right);
     if (old == -1)
       return;
-    ParentStep ps;
     int sib_lo, sib_hi;
     if (is_left_child)
     {
       range_right = old;
-      ps.left_child = node_num;
       sib_lo = p + 1;
       sib_hi = range_right;
       delta_right = seg_delta(codes, range_right, lo, hi);
@@ -171,7 +147,6 @@ __device__ void climb_global(const float *__restrict__ g, const uint32_t *__rest
     else
     {
       range_left = old;
-      ps.left_child = (p == range_left) ? p - lo : p - lo + num_internal + 1;
       sib_lo = range_left;
       sib_hi = p;
       delta_left = seg_delta(codes, range_left - 1, lo, hi);
@@ -187,52 +162,86 @@ __device__ void climb_global(const float *__restrict__ g, const uint32_t *__rest
     }
     else
     {
-      fence_acq_rel_gpu(); // acquire internal[sib_node]
-      sib = load_internal_box_cg(internal + sib_node);
+      fence_acq_rel_gpu(); // acquire tnodes[sib_node]
+      sib = load_tnode_box_cg(tnodes + sib_node);
     }
-    ps.kp = delta_right < delta_left ? range_right : range_left;
-    if (range_right != hi)
-      ps.rope = delta_right < seg_delta(codes, range_right + 1, lo, hi)
-                    ? range_right + 1 - lo
-                    : range_right + 1 - lo + num_internal + 1;
-    else
-      ps.rope = kRopeSentinel;
+    const int kp = delta_right < delta_left ? range_right : range_left;
     const int own_ref = cur_node < 0 ? bucket_ref(st.value) : cur_node;
     const int own_c = cur_node < 0 ? 1 : child_count_field(cur_node, own_lo, own_hi);
     const int sib_ref = sib_leaf ? bucket_ref(sib_value) : sib_node;
     const int sib_c = sib_leaf ? 1 : child_count_field(sib_node, sib_lo, sib_hi);
-    write_parent(tnodes, internal, ps, is_left_child, box, own_ref, own_c, sib, sib_ref, sib_c);
+    write_parent(tnodes, kp, is_left_child, box, own_ref, own_c, sib, sib_ref, sib_c);
     wrote = true;
-    cur_node = ps.kp;
-    node_num = ps.kp - lo + num_internal + 1;
+    cur_node = kp;
   }
+}
+
+// The second arriver at the flag of split p creates the parent of its node
+// [L, R] (slot `node`, -1 for the leaf L) and the sibling: writes the
+// parent's child-pair node and box, and moves (L, R, node) up to the parent.
+__device__ __forceinline__ void make_parent(TNode *__restrict__ tnodes, const long long *s_delta,
+                                            const Box3 *s_leaf, const int *s_value, Box3 *s_box,
+                                            int b0, bool is_left_child, int p, int old, int &L,
+                                            int &R, int &node)
+{
+  int nl = L, nr = R, sib_lo, sib_hi;
+  if (is_left_child)
+  {
+    nr = old;
+    sib_lo = p + 1;
+    sib_hi = nr;
+  }
+  else
+  {
+    nl = old;
+    sib_lo = nl;
+    sib_hi = p;
+  }
+  const int sib_node = is_left_child ? p + 1 : p;
+  const bool sib_leaf = sib_lo == sib_hi;
+  Box3 box = node < 0 ? s_leaf[L - b0] : s_box[node - b0];
+  const Box3 sib = sib_leaf ? s_leaf[sib_lo - b0] : s_box[sib_node - b0];
+  const int sib_ref = sib_leaf ? bucket_ref(s_value[sib_lo - b0]) : sib_node;
+  const int sib_c = sib_leaf ? 1 : child_count_field(sib_node, sib_lo, sib_hi);
+  const int own_ref = node < 0 ? bucket_ref(s_value[L - b0]) : node;
+  const int own_c = node < 0 ? 1 : child_count_field(node, L, R);
+  const int kp = s_delta[nr - b0 + 1] < s_delta[nl - b0] ? nr : nl;
+  write_parent(tnodes, kp, is_left_child, box, own_ref, own_c, sib, sib_ref, sib_c);
+  s_box[kp - b0] = box;
+  L = nl;
+  R = nr;
+  node = kp;
 }
 
 // Apetrei's climb, first regime.
 //
-// Each CTA owns kHierBlock consecutive positions [b0, b1].  While the parent a
-// thread climbs to covers only positions of its CTA, the flag exchange and the
-// sibling's box go through shared memory (block-scope fences, no global
-// atomics).  The parent of a node [L, R] lies inside the CTA iff its other
-// child ends inside it: for a left child (split p = R) iff some j in
-// [p + 1, b1] has delta(j) >= delta(p), for a right child (split p = L - 1)
-// iff some j in [b0 - 1, p - 1] has delta(j) > delta(p) -- read from suffix
-// and prefix maxima of the CTA's deltas (tree boundaries have delta = +inf).
-// Both children of a parent reach the same verdict, so they meet on the same
-// flag.  A thread whose parent leaves the CTA records its state in the
-// frontier list and stops, so the CTA retires at once; k_hierarchy_global
-// finishes those climbs (when the list is full the thread finishes its climb
-// with climb_global itself).  Nothing spins: the first arriver at a parent
-// stops.
+// Each CTA owns kHierBlock consecutive positions [b0, b1].  Work items are
+// the nodes whose parent is still to be reached: (range, node), the leaves
+// first.  In a round every item tries its parent's flag in shared memory; the
+// second arriver creates the parent, which is an item of the next round.
+// Every sibling an item reads was created in an earlier round, so the
+// barrier (or __syncwarp) between rounds orders all shared-memory boxes.  The
+// list is compacted every round while it holds more than 32 items (about
+// log2(kHierBlock / 32) rounds); warp 0 then finishes alone, one item per
+// lane, so idle warps do not cycle through the tail rounds.
 //
-// Every internal node gets its reference-layout record and its 64-byte
-// child-pair node; leaf geometry is copied into Morton order on the way.
+// The parent of a node [L, R] lies inside the CTA iff its other child ends
+// inside it: for a left child (split p = R) iff some j in [p + 1, b1] has
+// delta(j) >= delta(p), for a right child (split p = L - 1) iff some j in
+// [b0 - 1, p - 1] has delta(j) > delta(p) -- read from suffix and prefix
+// maxima of the CTA's deltas (tree boundaries have delta = +inf).  Both
+// children of a parent reach the same verdict, so they meet on the same
+// flag.  An item whose parent leaves the CTA goes to the frontier list,
+// finished by k_hierarchy_global (or in place when the list is full).
+//
+// Writes the 64-byte child-pair node of every internal node and the leaf
+// geometry in Morton order; the reference-layout arrays are derived from
+// them on demand (export_reference_layout).
 template <int KIND>
 __global__ void __launch_bounds__(kHierBlock)
     k_hierarchy_local(const float *__restrict__ g, int64_t total, const int64_t *__restrict__ off,
                       int nseg, const uint32_t *__restrict__ perm,
                       const uint64_t *__restrict__ codes, int *__restrict__ ranges,
-                      LeafNode *__restrict__ leaves, InternalNode *__restrict__ internal,
                       TNode *__restrict__ tnodes, float4 *__restrict__ sorted,
                       ClimbState *__restrict__ frontier, unsigned *__restrict__ frontier_count,
                       int frontier_capacity)
@@ -244,29 +253,37 @@ __global__ void __launch_bounds__(kHierBlock)
   __shared__ Box3 s_box[kHierBlock];           // internal node with slot in [b0, b1]
   __shared__ Box3 s_leaf[kHierBlock];
   __shared__ int s_value[kHierBlock];
+  __shared__ int3 s_items[2][kHierBlock];       // (range_left, range_right, node or -1)
+  __shared__ int s_count[2];
 
   const int b0 = blockIdx.x * kHierBlock;
   const int b1 = (int)min((int64_t)b0 + kHierBlock - 1, total - 1);
   const int nb = b1 - b0 + 1;
   const int tid = threadIdx.x;
+  const int lane = tid & 31;
 
   for (int k = tid; k <= nb; k += blockDim.x)
     s_delta[k] = pos_delta(codes, off, nseg, total, b0 - 1 + k);
   s_flag[tid] = -1;
+  if (tid < 2)
+    s_count[tid] = 0;
   const int i = b0 + tid;
-  Box3 box = empty_box();
-  int value = 0, lo = 0, hi = 0;
   if (i <= b1)
   {
     const int s = nseg > 1 ? find_segment(off, nseg, i) : 0;
-    lo = (int)__ldg(off + s);
-    hi = (int)__ldg(off + s + 1) - 1;
+    const int lo = (int)__ldg(off + s);
+    const int hi = (int)__ldg(off + s + 1) - 1;
     const int original = (int)__ldg(perm + i);
-    value = original - lo;
-    box = load_leaf_box<KIND>(g, original);
+    const int value = original - lo;
+    const Box3 box = load_leaf_box<KIND>(g, original);
     s_leaf[tid] = box;
     s_value[tid] = value;
     SortedLeaf<KIND>::store(sorted, i, box, value);
+    s_items[0][tid] = make_int3(i, i, -1);
+    if (lo == hi)
+      // one-leaf tree (ArborX_TreeConstruction.hpp:41-69): a one-leaf
+      // bucket on the left, nothing on the right (count 0)
+      tnodes[lo] = make_tnode(box, bucket_ref(value), 1, empty_box(), bucket_ref(0), 0);
   }
   __syncthreads();
   // inclusive prefix maxima s_pre[k] = max(s_delta[0..k]) and suffix maxima
@@ -275,7 +292,7 @@ __global__ void __launch_bounds__(kHierBlock)
   {
     __shared__ long long w_pre[kHierBlock / 32];
     __shared__ long long w_suf[kHierBlock / 32];
-    const int lane = tid & 31, warp = tid >> 5;
+    const int warp = tid >> 5;
     const long long v = tid <= nb ? s_delta[tid] : LLONG_MIN;
     long long pre = v, suf = v;
 #pragma unroll
@@ -311,124 +328,218 @@ __global__ void __launch_bounds__(kHierBlock)
     }
     __syncthreads();
   }
-  if (i > b1)
-    return;
 
-  const int num_internal = hi - lo; // tree-local
-  // delta(j) for j in [b0 - 1, b1]
-  auto delta_at = [&](int j) -> long long { return s_delta[j - b0 + 1]; };
-  // GenerateHierarchy::setRope (ArborX_TreeConstruction.hpp:173-195) in
-  // tree-local node numbers
-  auto rope_of = [&](int range_right, long long delta_right) -> int {
-    if (range_right == hi)
-      return kRopeSentinel;
-    const long long next = range_right + 1 <= b1 ? delta_at(range_right + 1)
-                                                  : seg_delta(codes, range_right + 1, lo, hi);
-    return delta_right < next ? range_right + 1 - lo : range_right + 1 - lo + num_internal + 1;
-  };
-
-  int range_left = i, range_right = i;
-  long long delta_left = delta_at(range_left - 1);
-  long long delta_right = delta_at(range_right);
-  LeafNode leaf;
-  leaf.rope = rope_of(range_right, delta_right);
-  leaf.value = value;
-  leaves[i] = leaf;
-  if (lo == hi)
-  {
-    // one-leaf tree (ArborX_TreeConstruction.hpp:41-69): a one-leaf bucket on
-    // the left, nothing on the right (count 0)
-    tnodes[lo] = make_tnode(box, bucket_ref(value), 1, empty_box(), bucket_ref(0), 0);
-    return;
-  }
-
-  int cur_node = -1;        // slot of the node this thread completed last
-  int node_num = i - lo;    // its tree-local node number
-  while (!(range_left == lo && range_right == hi))
-  {
-    const bool is_left_child = delta_right < delta_left;
-    const int p = is_left_child ? range_right : range_left - 1;
-    const bool inside = is_left_child ? (p < b1 && s_suf[p - b0 + 2] >= delta_right)
-                                      : (p >= b0 && s_pre[p - b0] > delta_left);
+  // One climb step of the item (L, R, node): returns true when the item
+  // moves up to the parent it created.
+  auto step = [&](int &L, int &R, int &node) -> bool {
+    const long long dl = s_delta[L - b0];
+    const long long dr = s_delta[R - b0 + 1];
+    if (dl == LLONG_MAX && dr == LLONG_MAX) // the root of a tree
+      return false;
+    const bool is_left_child = dr < dl;
+    const int p = is_left_child ? R : L - 1;
+    const bool inside = is_left_child ? (p < b1 && s_suf[p - b0 + 2] >= dr)
+                                      : (p >= b0 && s_pre[p - b0] > dl);
     if (!inside)
     {
+      const Box3 box = node < 0 ? s_leaf[L - b0] : s_box[node - b0];
       ClimbState st;
-      st.range_left = range_left;
-      st.range_right = range_right;
-      st.cur_node = cur_node;
-      st.node_num = node_num;
-      st.value = value;
-      st.lo = lo;
-      st.hi = hi;
-      st.pad = 0;
+      st.range_left = L;
+      st.range_right = R;
+      st.cur_node = node;
+      st.value = node < 0 ? s_value[L - b0] : 0;
+      const int s = nseg > 1 ? find_segment(off, nseg, L) : 0;
+      st.lo = (int)__ldg(off + s);
+      st.hi = (int)__ldg(off + s + 1) - 1;
+      st.pad[0] = st.pad[1] = 0;
 #pragma unroll
       for (int d = 0; d < 3; ++d)
       {
         st.blo[d] = box.lo[d];
         st.bhi[d] = box.hi[d];
       }
+      st.pad2[0] = st.pad2[1] = 0.f;
       const unsigned slot = atomicAdd(frontier_count, 1u);
       if ((int)slot < frontier_capacity)
         frontier[slot] = st;
       else // list full (very deep trees): finish this climb here
-        climb_global<KIND>(g, perm, codes, ranges, internal, tnodes, st, cur_node >= 0);
-      return;
+        climb_global<KIND>(g, perm, codes, ranges, tnodes, st, true);
+      return false;
     }
-    const int own_lo = range_left, own_hi = range_right;
-    __threadfence_block(); // release s_box[cur_node - b0]
-    const int old = atomicCAS(s_flag + (p - b0), -1, is_left_child ? range_left : range_right);
+    const int old = atomicCAS(s_flag + (p - b0), -1, is_left_child ? L : R);
     if (old == -1)
-      return;
-    __threadfence_block(); // acquire the sibling's s_box entry
-    ParentStep ps;
-    int sib_lo, sib_hi;
-    if (is_left_child)
+      return false;
+    make_parent(tnodes, s_delta, s_leaf, s_value, s_box, b0, is_left_child, p, old, L, R, node);
+    return true;
+  };
+
+  // CTA-wide rounds over a compacted item list while it holds more than a
+  // warp's worth of items
+  int cur = 0;
+  int count = nb;
+  while (count > 32)
+  {
+    bool emit = false;
+    int L = 0, R = 0, node = -1;
+    if (tid < count)
     {
-      range_right = old;
-      ps.left_child = node_num;
-      sib_lo = p + 1;
-      sib_hi = range_right;
-      delta_right = delta_at(range_right);
+      const int3 it = s_items[cur][tid];
+      L = it.x;
+      R = it.y;
+      node = it.z;
+      emit = step(L, R, node);
     }
-    else
+    const int nxt = cur ^ 1;
+    const unsigned mask = __ballot_sync(0xffffffffu, emit);
+    if (mask)
     {
-      range_left = old;
-      ps.left_child = (p == range_left) ? p - lo : p - lo + num_internal + 1;
-      sib_lo = range_left;
-      sib_hi = p;
-      delta_left = delta_at(range_left - 1);
+      const int leader = __ffs(mask) - 1;
+      int base = 0;
+      if (lane == leader)
+        base = atomicAdd(&s_count[nxt], __popc(mask));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (emit)
+        s_items[nxt][base + __popc(mask & lanemask_lt())] = make_int3(L, R, node);
     }
-    const int sib_node = is_left_child ? p + 1 : p;
-    const bool sib_leaf = (sib_lo == sib_hi);
-    const Box3 sib = sib_leaf ? s_leaf[sib_lo - b0] : s_box[sib_node - b0];
-    const int sib_value = sib_leaf ? s_value[sib_lo - b0] : 0;
-    ps.kp = delta_right < delta_left ? range_right : range_left;
-    ps.rope = rope_of(range_right, delta_right);
-    const int own_ref = cur_node < 0 ? bucket_ref(value) : cur_node;
-    const int own_c = cur_node < 0 ? 1 : child_count_field(cur_node, own_lo, own_hi);
-    const int sib_ref = sib_leaf ? bucket_ref(sib_value) : sib_node;
-    const int sib_c = sib_leaf ? 1 : child_count_field(sib_node, sib_lo, sib_hi);
-    write_parent(tnodes, internal, ps, is_left_child, box, own_ref, own_c, sib, sib_ref, sib_c);
-    s_box[ps.kp - b0] = box;
-    cur_node = ps.kp;
-    node_num = ps.kp - lo + num_internal + 1;
+    __syncthreads();
+    count = s_count[nxt];
+    if (tid == 0)
+      s_count[cur] = 0;
+    cur = nxt;
+    __syncthreads();
+  }
+  // the rest by warp 0 alone: one item per lane, warp-synchronous rounds
+  if (tid >= 32)
+    return;
+  int L = 0, R = 0, node = -1;
+  bool active = lane < count;
+  if (active)
+  {
+    const int3 it = s_items[cur][lane];
+    L = it.x;
+    R = it.y;
+    node = it.z;
+  }
+  while (__any_sync(0xffffffffu, active))
+  {
+    if (active)
+      active = step(L, R, node);
+    __syncwarp();
   }
 }
 
-// Second regime: the climbs handed over by k_hierarchy_local.  Their node
-// records were written by the previous kernel.
+// Second regime: the climbs handed over by k_hierarchy_local.  Their nodes
+// were written by the previous kernel.
 template <int KIND>
 __global__ void __launch_bounds__(256)
     k_hierarchy_global(const float *__restrict__ g, const uint32_t *__restrict__ perm,
                        const uint64_t *__restrict__ codes, int *__restrict__ ranges,
-                       InternalNode *__restrict__ internal, TNode *__restrict__ tnodes,
-                       const ClimbState *__restrict__ frontier,
+                       TNode *__restrict__ tnodes, const ClimbState *__restrict__ frontier,
                        const unsigned *__restrict__ frontier_count, int capacity)
 {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= min((int)*frontier_count, capacity))
     return;
-  climb_global<KIND>(g, perm, codes, ranges, internal, tnodes, frontier[e], false);
+  climb_global<KIND>(g, perm, codes, ranges, tnodes, frontier[e], false);
+}
+
+// ---------------------------------------------------------------------------
+// Reference-layout node arrays, derived from the child-pair nodes
+// ---------------------------------------------------------------------------
+
+// Leaf values in Morton order and their inverse (value -> leaf number).
+template <int KIND>
+__global__ void k_export_values(const float4 *__restrict__ sorted, int64_t lo, int n,
+                                LeafNode *__restrict__ leaves, int *__restrict__ inv,
+                                unsigned *__restrict__ err)
+{
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n)
+    return;
+  Box3 b;
+  int v;
+  SortedLeaf<KIND>::load(sorted, lo + p, b, v);
+  leaves[p].value = v;
+  if (n == 1)
+    leaves[p].rope = kRopeSentinel;
+  if ((unsigned)v < (unsigned)n)
+    inv[v] = p;
+  else
+    raise_error(err, ABX_DEVERR_INTERNAL);
+}
+
+// Node number of a child reference of the tree whose slots start at lo.
+__device__ __forceinline__ int child_number(int ref, int64_t lo, int n, const int *__restrict__ inv)
+{
+  return ref >= 0 ? (int)(ref - lo) + n : inv[bucket_start(ref)];
+}
+
+// Left child, box and parent links of every internal node (Karras index k,
+// node number n + k; ArborX_HappyTreeFriends.hpp:23-86 numbering).
+__global__ void k_export_internal(const TNode *__restrict__ tnodes, int64_t lo, int n,
+                                  const int *__restrict__ inv, InternalNode *__restrict__ internal,
+                                  int *__restrict__ parent, int *__restrict__ right,
+                                  unsigned *__restrict__ err)
+{
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n - 1)
+    return;
+  const TNode t = tnodes[lo + k];
+  Box3 l, r;
+  tnode_children(t, l, r);
+  expand(l, r);
+  const int lc = child_number(t.d.x, lo, n, inv);
+  const int rc = child_number(t.d.y, lo, n, inv);
+  if ((unsigned)lc >= (unsigned)(2 * n - 1) || (unsigned)rc >= (unsigned)(2 * n - 1))
+  {
+    raise_error(err, ABX_DEVERR_INTERNAL);
+    return;
+  }
+  InternalNode node;
+  node.left_child = lc;
+  node.rope = kRopeSentinel;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    node.lo[d] = l.lo[d];
+    node.hi[d] = l.hi[d];
+  }
+  internal[k] = node;
+  parent[lc] = 2 * k;
+  parent[rc] = 2 * k + 1;
+  right[k] = rc;
+}
+
+// Ropes (GenerateHierarchy::setRope, ArborX_TreeConstruction.hpp:173-195):
+// the rope of a node is the right sibling of its nearest ancestor-or-self
+// that is a left child; the sentinel when there is none.
+__global__ void k_export_ropes(int n, const int *__restrict__ parent, const int *__restrict__ right,
+                               LeafNode *__restrict__ leaves, InternalNode *__restrict__ internal,
+                               unsigned *__restrict__ err)
+{
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= 2 * n - 1)
+    return;
+  int y = x, rope = kRopeSentinel;
+  for (int steps = 0; y != n; ++steps)
+  {
+    const int e = parent[y];
+    if (steps > 2 * n || (unsigned)(e >> 1) >= (unsigned)(n - 1))
+    {
+      raise_error(err, ABX_DEVERR_INTERNAL);
+      break;
+    }
+    if ((e & 1) == 0)
+    {
+      rope = right[e >> 1];
+      break;
+    }
+    y = (e >> 1) + n;
+  }
+  if (x < n)
+    leaves[x].rope = rope;
+  else
+    internal[x - n].rope = rope;
 }
 
 // ---------------------------------------------------------------------------
@@ -595,7 +706,6 @@ __global__ void k_one_segment(int64_t *off, int64_t n)
 abx_status generate_hierarchy_segments(cudaStream_t s, abx_geometry kind, const float *d_g,
                                        int64_t total, const int64_t *d_off, int nseg,
                                        const uint32_t *d_perm, const uint64_t *d_codes,
-                                       LeafNode *d_leaves, InternalNode *d_internal,
                                        TNode *d_tnodes, float4 *d_sorted)
 {
   if (total < 1)
@@ -612,7 +722,7 @@ abx_status generate_hierarchy_segments(cudaStream_t s, abx_geometry kind, const 
     d_sorted = tmp_sorted.ptr;
   }
   const unsigned blocks = (unsigned)((total + kHierBlock - 1) / kHierBlock);
-  // a CTA's positions split into a few maximal subtrees (2 log2(512) + 2 for
+  // a CTA's positions split into a few maximal subtrees (2 log2(kHierBlock) + 2 for
   // a balanced tree), each handing over at most one climb; deeper trees that
   // overflow the list finish those climbs in the first kernel
   const int capacity = (int)blocks * 24;
@@ -625,19 +735,19 @@ abx_status generate_hierarchy_segments(cudaStream_t s, abx_geometry kind, const 
   StageScope scope(s, "hierarchy", 2);
   if (kind == ABX_POINT)
   {
-    k_hierarchy_local<0><<<blocks, kHierBlock, 0, s>>>(
-        d_g, total, d_off, nseg, d_perm, d_codes, ranges.ptr, d_leaves, d_internal, d_tnodes,
-        d_sorted, frontier.ptr, count.ptr, capacity);
-    k_hierarchy_global<0><<<gblocks, 256, 0, s>>>(d_g, d_perm, d_codes, ranges.ptr, d_internal,
-                                                  d_tnodes, frontier.ptr, count.ptr, capacity);
+    k_hierarchy_local<0><<<blocks, kHierBlock, 0, s>>>(d_g, total, d_off, nseg, d_perm, d_codes,
+                                                       ranges.ptr, d_tnodes, d_sorted,
+                                                       frontier.ptr, count.ptr, capacity);
+    k_hierarchy_global<0><<<gblocks, 256, 0, s>>>(d_g, d_perm, d_codes, ranges.ptr, d_tnodes,
+                                                  frontier.ptr, count.ptr, capacity);
   }
   else
   {
-    k_hierarchy_local<1><<<blocks, kHierBlock, 0, s>>>(
-        d_g, total, d_off, nseg, d_perm, d_codes, ranges.ptr, d_leaves, d_internal, d_tnodes,
-        d_sorted, frontier.ptr, count.ptr, capacity);
-    k_hierarchy_global<1><<<gblocks, 256, 0, s>>>(d_g, d_perm, d_codes, ranges.ptr, d_internal,
-                                                  d_tnodes, frontier.ptr, count.ptr, capacity);
+    k_hierarchy_local<1><<<blocks, kHierBlock, 0, s>>>(d_g, total, d_off, nseg, d_perm, d_codes,
+                                                       ranges.ptr, d_tnodes, d_sorted,
+                                                       frontier.ptr, count.ptr, capacity);
+    k_hierarchy_global<1><<<gblocks, 256, 0, s>>>(d_g, d_perm, d_codes, ranges.ptr, d_tnodes,
+                                                  frontier.ptr, count.ptr, capacity);
   }
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
@@ -656,16 +766,67 @@ abx_status generate_hierarchy(cudaStream_t s, abx_geometry kind, const float *d_
     ABX_CUDA_TRY(tmp_t.alloc(n, s));
     d_tnodes = tmp_t.ptr;
   }
+  Scratch<float4> tmp_sorted;
+  if (!d_sorted)
+  {
+    ABX_CUDA_TRY(tmp_sorted.alloc((size_t)n * (kind == ABX_BOX ? 2 : 1), s));
+    d_sorted = tmp_sorted.ptr;
+  }
   Scratch<int64_t> off;
   ABX_CUDA_TRY(off.alloc(2, s));
   k_one_segment<<<1, 1, 0, s>>>(off.ptr, n);
-  return generate_hierarchy_segments(s, kind, d_g, n, off.ptr, 1, d_perm, d_codes, d_leaves,
-                                     d_internal, d_tnodes, d_sorted);
+  ABX_TRY(generate_hierarchy_segments(s, kind, d_g, n, off.ptr, 1, d_perm, d_codes, d_tnodes,
+                                      d_sorted));
+  if (d_leaves || d_internal)
+    ABX_TRY(export_reference_layout(s, kind, d_tnodes, d_sorted, 0, n, d_leaves, d_internal));
+  return ABX_SUCCESS;
+}
+
+abx_status export_reference_layout(cudaStream_t s, abx_geometry kind, const TNode *d_tnodes,
+                                   const float4 *d_sorted, int64_t lo, int64_t n,
+                                   LeafNode *d_leaves, InternalNode *d_internal)
+{
+  if (n <= 0)
+    return ABX_SUCCESS;
+  if (n > (int64_t)INT32_MAX / 2)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "export: too many values");
+  DeviceState &ds = device_state();
+  Scratch<LeafNode> tmp_leaves;
+  Scratch<InternalNode> tmp_internal;
+  if (!d_leaves)
+  {
+    ABX_CUDA_TRY(tmp_leaves.alloc(n, s));
+    d_leaves = tmp_leaves.ptr;
+  }
+  if (!d_internal && n > 1)
+  {
+    ABX_CUDA_TRY(tmp_internal.alloc(n - 1, s));
+    d_internal = tmp_internal.ptr;
+  }
+  const int nn = (int)n;
+  Scratch<int> inv, parent, right;
+  ABX_CUDA_TRY(inv.alloc(n, s));
+  const unsigned b1 = (unsigned)((n + 255) / 256);
+  if (kind == ABX_BOX)
+    k_export_values<1><<<b1, 256, 0, s>>>(d_sorted, lo, nn, d_leaves, inv.ptr, ds.d_error);
+  else
+    k_export_values<0><<<b1, 256, 0, s>>>(d_sorted, lo, nn, d_leaves, inv.ptr, ds.d_error);
+  ABX_CUDA_TRY(cudaGetLastError());
+  if (n == 1)
+    return ABX_SUCCESS;
+  ABX_CUDA_TRY(parent.alloc(2 * n - 1, s));
+  ABX_CUDA_TRY(right.alloc(n - 1, s));
+  k_export_internal<<<(unsigned)((n - 1 + 255) / 256), 256, 0, s>>>(
+      d_tnodes, lo, nn, inv.ptr, d_internal, parent.ptr, right.ptr, ds.d_error);
+  k_export_ropes<<<(unsigned)((2 * n - 1 + 255) / 256), 256, 0, s>>>(
+      nn, parent.ptr, right.ptr, d_leaves, d_internal, ds.d_error);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
 }
 
 abx_status forest_build(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t total,
-                        const int64_t *d_off, int nseg, float *d_bounds, LeafNode *d_leaves,
-                        InternalNode *d_internal, TNode *d_tnodes, float4 *d_sorted)
+                        const int64_t *d_off, int nseg, float *d_bounds, TNode *d_tnodes,
+                        float4 *d_sorted)
 {
   if (nseg < 1)
     return ABX_SUCCESS;
@@ -718,7 +879,7 @@ abx_status forest_build(cudaStream_t s, abx_geometry kind, const float *d_g, int
     ABX_CUDA_TRY(cudaGetLastError());
   }
   return generate_hierarchy_segments(s, kind, d_g, total, d_off, nseg, final_perm, codes.ptr,
-                                     d_leaves, d_internal, d_tnodes, d_sorted);
+                                     d_tnodes, d_sorted);
 }
 
 abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const float *d_preds,
