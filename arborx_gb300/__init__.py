@@ -13,6 +13,7 @@ pointers and results are zero-copy views of the library's own buffers.
 """
 
 from ._lib import AbxError, SearchException  # noqa: F401
+from .serve import Server  # noqa: F401
 from .bvh import (  # noqa: F401
     BoundingVolumeHierarchy,
     Forest,

@@ -39,6 +39,25 @@ class TraversalPolicyC(ctypes.Structure):
     _fields_ = [("buffer_size", ctypes.c_int32), ("sort_predicates", ctypes.c_int32)]
 
 
+class ServerConfigC(ctypes.Structure):
+    _fields_ = [("workers", ctypes.c_int32), ("reserved", ctypes.c_int32),
+                ("max_inflight_bytes", ctypes.c_int64), ("max_batch_queries", ctypes.c_int64)]
+
+
+class RequestC(ctypes.Structure):
+    _fields_ = [("tree", ctypes.c_int32), ("kind", ctypes.c_int32), ("h_queries", ctypes.c_void_p),
+                ("nq", ctypes.c_int64), ("k", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class ServerStatisticsC(ctypes.Structure):
+    _fields_ = [("completed_requests", ctypes.c_int64), ("completed_queries", ctypes.c_int64),
+                ("batches", ctypes.c_int64), ("p50_ms", ctypes.c_double), ("p99_ms", ctypes.c_double),
+                ("span_s", ctypes.c_double)]
+
+
+REQ_NEAREST = 0
+REQ_INTERSECTS = 1
+
 SIGNATURES = {
     "abx_status_string": (ctypes.c_char_p, [_STATUS]),
     "abx_last_error": (ctypes.c_char_p, []),
@@ -78,6 +97,14 @@ SIGNATURES = {
         _STATUS,
         [_P, _P, _P, _P, _P, _I32, TraversalPolicyC, _I32, ctypes.POINTER(_P)],
     ),
+    "abx_server_create": (_STATUS, [ctypes.POINTER(ServerConfigC), ctypes.POINTER(_P)]),
+    "abx_server_destroy": (_STATUS, [_P]),
+    "abx_server_add_tree": (_STATUS, [_P, _P, ctypes.POINTER(_I32)]),
+    "abx_server_submit": (_STATUS, [_P, ctypes.POINTER(RequestC), ctypes.POINTER(_I64)]),
+    "abx_server_wait": (_STATUS, [_P, _I64, ctypes.POINTER(_I64), ctypes.POINTER(ctypes.c_double)]),
+    "abx_server_result": (_STATUS, [_P, _I64, _P, _P, _P]),
+    "abx_server_stats": (_STATUS, [_P, ctypes.POINTER(ServerStatisticsC)]),
+    "abx_server_reset_stats": (_STATUS, [_P]),
     "abx_crs_num_queries": (_I64, [_P]),
     "abx_crs_num_results": (_I64, [_P]),
     "abx_crs_offsets": (_P, [_P]),

@@ -28,7 +28,9 @@ NVCC_FLAGS = ARCH + [
     "-I" + INCLUDE,
 ]
 
-SOURCES = ["abx_capi.cu", "abx_build.cu", "abx_hierarchy.cu", "abx_sort.cu", "abx_query.cu"]
+SOURCES = [
+    "abx_capi.cu", "abx_build.cu", "abx_hierarchy.cu", "abx_sort.cu", "abx_query.cu", "abx_serve.cu",
+]
 
 
 def _nvcc():

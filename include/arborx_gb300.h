@@ -262,6 +262,67 @@ ABX_API abx_status abx_forest_query_nearest(const abx_forest *forest,
                                             int32_t with_distances,
                                             abx_crs **out);
 
+/* ---------------------------------------------------------------------- */
+/* Serving: a request loop over trees resident in HBM                      */
+/* ---------------------------------------------------------------------- */
+/* No counterpart in the reference (it is the loop around
+ * BoundingVolumeHierarchy::query, ArborX_LinearBVH.hpp:90-110).  Worker
+ * threads, each on its own CUDA stream, coalesce the pending requests on one
+ * tree and of one kind into a single query launch (mixed k and radii
+ * allowed), admit batches while their device memory fits
+ * max_inflight_bytes, and run up to `workers` batches at once; requests that
+ * arrive meanwhile join the next batch.  A request's results are those of
+ * the same query run alone: nearest as abx_bvh_query_nearest (with
+ * distances), intersects as abx_bvh_query_intersects on spheres. */
+typedef struct abx_server abx_server;
+
+#define ABX_REQ_NEAREST 0    /* h_queries: nq points (3 floats), k          */
+#define ABX_REQ_INTERSECTS 1 /* h_queries: nq spheres (4 floats: x y z r)   */
+
+typedef struct abx_server_config
+{
+  int32_t workers;            /* concurrent batches (streams), default 4      */
+  int32_t reserved;
+  int64_t max_inflight_bytes; /* device-memory budget of running batches      */
+  int64_t max_batch_queries;  /* cap of one coalesced launch                  */
+} abx_server_config;
+
+typedef struct abx_request
+{
+  int32_t tree;             /* id from abx_server_add_tree                  */
+  int32_t kind;             /* ABX_REQ_NEAREST or ABX_REQ_INTERSECTS        */
+  const float *h_queries;   /* host rows; copied by abx_server_submit       */
+  int64_t nq;
+  int32_t k;                /* nearest only                                  */
+  int32_t reserved;
+} abx_request;
+
+typedef struct abx_server_statistics
+{
+  int64_t completed_requests;
+  int64_t completed_queries;
+  int64_t batches;          /* coalesced launches                            */
+  double p50_ms;            /* request latency, submit to completion        */
+  double p99_ms;
+  double span_s;            /* first submit to last completion               */
+} abx_server_statistics;
+
+/* cfg may be NULL (defaults: 4 workers, 8 GiB, 2^20 queries per launch). */
+ABX_API abx_status abx_server_create(const abx_server_config *cfg, abx_server **out);
+ABX_API abx_status abx_server_destroy(abx_server *srv);
+/* The tree must outlive the server. */
+ABX_API abx_status abx_server_add_tree(abx_server *srv, const abx_bvh *tree, int32_t *tree_id);
+ABX_API abx_status abx_server_submit(abx_server *srv, const abx_request *req, int64_t *ticket);
+/* Blocks until the request completed; its number of results and latency. */
+ABX_API abx_status abx_server_wait(abx_server *srv, int64_t ticket, int64_t *num_results,
+                                   double *latency_ms);
+/* Copies the results to host arrays (offsets nq + 1, indices, distances for
+ * nearest; any may be NULL) and releases the request. */
+ABX_API abx_status abx_server_result(abx_server *srv, int64_t ticket, int32_t *h_offsets,
+                                     int32_t *h_indices, float *h_distances);
+ABX_API abx_status abx_server_stats(abx_server *srv, abx_server_statistics *out);
+ABX_API abx_status abx_server_reset_stats(abx_server *srv);
+
 /* Accessors of a CRS result: device offsets (nq + 1), device indices
  * (num_results), device distances (nearest only, else NULL). */
 ABX_API int64_t abx_crs_num_queries(const abx_crs *crs);
