@@ -58,9 +58,13 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1_000_000,
                     help="queries timed per CPU step (scaled to --nq)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--dist", default="uniform", choices=["uniform", "clustered"],
+                    help="--case build/nearest/radius: point distribution")
+    ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[500, 2000, 8000, 32000])
     ap.add_argument("--clouds", type=int, default=4096,
                     help="--case forest: number of point clouds (trees)")
-    ap.add_argument("--case", default="knn", choices=["knn", "build", "nearest", "radius", "forest"],
+    ap.add_argument("--case", default="knn", choices=["knn", "build", "nearest", "radius", "forest", "serve"],
                     help="knn: the benchmark step (build + kNN); build / nearest / radius: "
                     "one stage alone (profiling cases; radius = 2-pass CRS search with "
                     "~32 expected neighbours)")
@@ -74,7 +78,22 @@ def dist_env():
     return rank, world, local
 
 
-def make_inputs(n, nq, rank):
+def clustered(n, seed_pick, seed_offset):
+    """Gaussian mixture of 64 components: centres U[0,1)^3 (seed 5), sigma =
+    10^U(-3,-1) (seed 6), weights Dirichlet(1) (seed 7), component per point
+    by CDF search, N(0, sigma^2 I) offsets, no clipping."""
+    centres = np.random.default_rng(5).random((64, 3))
+    sigma = 10.0 ** np.random.default_rng(6).uniform(-3, -1, 64)
+    w = np.random.default_rng(7).dirichlet(np.ones(64))
+    comp = np.searchsorted(np.cumsum(w), np.random.default_rng(seed_pick).random(n), side="right")
+    comp = np.minimum(comp, 63)
+    off = np.random.default_rng(seed_offset).normal(0.0, 1.0, (n, 3)) * sigma[comp, None]
+    return (centres[comp] + off).astype(np.float32)
+
+
+def make_inputs(n, nq, rank, dist="uniform"):
+    if dist == "clustered":
+        return clustered(n, 8 + 1000 * rank, 9 + 1000 * rank), clustered(nq, 10 + 1000 * rank, 11 + 1000 * rank)
     rng_p = np.random.default_rng(3 + 1000 * rank)
     rng_q = np.random.default_rng(12 + 1000 * rank)
     return rng_p.random((n, 3), dtype=np.float32), rng_q.random((nq, 3), dtype=np.float32)
@@ -493,7 +512,7 @@ def run_case(args):
 
     libbuild.build()
     L = _lib.load()
-    points_np, queries_np = make_inputs(args.n, args.nq, 0)
+    points_np, queries_np = make_inputs(args.n, args.nq, 0, args.dist)
     points = torch.from_numpy(points_np).cuda()
     queries = torch.from_numpy(queries_np).cuda()
     r = float(np.float32((32 * 3 / (4 * np.pi * args.n)) ** (1 / 3)))
@@ -531,7 +550,7 @@ def run_case(args):
             stages[name] = t.value / args.steps
     units = args.n if args.case == "build" else args.nq
     print(json.dumps({
-        "case": args.case, "n": args.n, "nq": args.nq, "k": args.k, "ms_per_step": ms,
+        "case": args.case, "dist": args.dist, "n": args.n, "nq": args.nq, "k": args.k, "ms_per_step": ms,
         "value": units / (ms * 1e-3), "unit": "points/s" if args.case == "build" else "queries/s",
         "stages_ms": stages,
     }), flush=True)
@@ -623,12 +642,88 @@ def run_forest(args):
         sys.exit(1)
 
 
+def run_serve(args):
+    """Serving workload: 64 resident trees of floor(10^U(5,7)) uniform points
+    (seed 16); Poisson arrivals at a fixed offered rate (swept); each request
+    picks a tree uniformly, is nearest(k), k in {1, 8, 32}, or a radius query
+    with r for about 32 hits at that tree's density, with equal odds, and
+    carries floor(10^U(0,5)) queries.  Reports achieved queries/s and the
+    p50 / p99 request latency (submit to completion) per offered rate."""
+    import torch
+
+    import arborx_gb300 as ax
+    from arborx_gb300 import build as libbuild
+
+    libbuild.build()
+    ntrees = args.clouds if args.clouds != 4096 else 64
+    sizes = np.floor(10.0 ** np.random.default_rng(16).uniform(5, 7, ntrees)).astype(np.int64)
+    trees = []
+    for j, n in enumerate(sizes):
+        pts = torch.rand((int(n), 3), generator=torch.Generator(device="cuda").manual_seed(1000 + j),
+                         device="cuda")
+        trees.append(ax.BoundingVolumeHierarchy(pts))
+    torch.cuda.synchronize()
+    srv = ax.Server(workers=4)
+    tids = [srv.add_tree(t) for t in trees]
+    radius = (32 * 3 / (4 * np.pi * sizes.astype(np.float64))) ** (1 / 3)
+    rng = np.random.default_rng(17)
+    pool = []
+    for _ in range(args.serve_requests):
+        t = int(rng.integers(0, ntrees))
+        nq = int(np.floor(10 ** rng.uniform(0, 5)))
+        c = rng.random((nq, 3), dtype=np.float32)
+        if rng.random() < 0.5:
+            pool.append((t, "nearest", c, int(rng.choice([1, 8, 32]))))
+        else:
+            r = np.full((nq, 1), np.float32(radius[t]), np.float32)
+            pool.append((t, "intersects", np.concatenate([c, r], axis=1), 0))
+
+    def submit(req):
+        t, kind, rows, k = req
+        if kind == "nearest":
+            return srv.submit_nearest(tids[t], rows, k)
+        return srv.submit_intersects(tids[t], rows)
+
+    for req in pool[:16]:  # warm-up
+        srv.result(submit(req))
+    sweep = []
+    for rate in args.serve_rates:
+        srv.reset_stats()
+        gaps = np.random.default_rng(int(rate)).exponential(1.0 / rate, len(pool))
+        tickets = []
+        t0 = time.perf_counter()
+        due = t0
+        for req, gap in zip(pool, gaps):
+            due += gap
+            while time.perf_counter() < due:
+                pass
+            tickets.append(submit(req))
+        for tk in tickets:
+            srv.wait(tk)
+        span = time.perf_counter() - t0
+        st = srv.stats()
+        for tk in tickets:
+            srv.result(tk)
+        sweep.append({
+            "offered_rps": rate, "achieved_rps": len(pool) / span,
+            "queries_per_s": st["completed_queries"] / span, "p50_ms": st["p50_ms"],
+            "p99_ms": st["p99_ms"], "launches": st["batches"], "requests": len(pool),
+        })
+    srv.close()
+    print(json.dumps({
+        "case": "serve", "trees": ntrees, "points": int(sizes.sum()), "workers": 4,
+        "requests_per_rate": len(pool), "sweep": sweep,
+    }), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.case == "forest":
         run_forest(args)
+    elif args.case == "serve":
+        run_serve(args)
     elif args.case != "knn":
         run_case(args)
     else:
