@@ -16,6 +16,7 @@ from ._lib import AbxError, SearchException  # noqa: F401
 from .serve import Server  # noqa: F401
 from .bvh import (  # noqa: F401
     BoundingVolumeHierarchy,
+    BruteForce,
     Forest,
     Intersects,
     Nearest,

@@ -97,6 +97,18 @@ SIGNATURES = {
         _STATUS,
         [_P, _P, _P, _P, _P, _I32, TraversalPolicyC, _I32, ctypes.POINTER(_P)],
     ),
+    "abx_brute_create": (_STATUS, [_P, ctypes.c_int, _P, _I64, ctypes.POINTER(_P)]),
+    "abx_brute_destroy": (_STATUS, [_P]),
+    "abx_brute_size": (_I64, [_P]),
+    "abx_brute_bounds": (_STATUS, [_P, _P]),
+    "abx_brute_query_intersects": (
+        _STATUS,
+        [_P, _P, ctypes.c_int, _P, _I64, TraversalPolicyC, ctypes.POINTER(_P)],
+    ),
+    "abx_brute_query_nearest": (
+        _STATUS,
+        [_P, _P, _P, _I64, _P, _I32, TraversalPolicyC, _I32, ctypes.POINTER(_P)],
+    ),
     "abx_server_create": (_STATUS, [ctypes.POINTER(ServerConfigC), ctypes.POINTER(_P)]),
     "abx_server_destroy": (_STATUS, [_P]),
     "abx_server_add_tree": (_STATUS, [_P, _P, ctypes.POINTER(_I32)]),

@@ -211,6 +211,48 @@ class BoundingVolumeHierarchy:
 BVH = BoundingVolumeHierarchy
 
 
+class BruteForce:
+    """ArborX::BruteForce (src/spatial/ArborX_BruteForce.hpp:40-176): every
+    predicate against every value.  Same query API as the tree; nearest results
+    equal the tree's, intersects results come in ascending value order."""
+
+    _prefix = "abx_brute"
+
+    def __init__(self, values, space=None, kind=None):
+        L = _lib.load()
+        self._h = ctypes.c_void_p()
+        if kind is None:
+            kind = {3: POINT, 6: BOX}.get(values.shape[-1])
+            if kind is None:
+                raise ValueError("values must have 3 (point) or 6 (box) columns")
+        self.kind = kind
+        v = _as_rows(values, 3 if kind == POINT else 6, "values")
+        check(L.abx_brute_create(_stream(space), kind, _ptr(v), v.shape[0], ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.load().abx_brute_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def size(self):
+        return int(_lib.load().abx_brute_size(self._h))
+
+    def empty(self):
+        return self.size() == 0
+
+    def bounds(self):
+        out = (ctypes.c_float * 6)()
+        check(_lib.load().abx_brute_bounds(self._h, out))
+        return tuple(out)
+
+    def query(self, predicates, policy=None, space=None, with_distances=False):
+        return query(self, predicates, policy, space=space, with_distances=with_distances)
+
+
 def query(tree, predicates, policy=None, space=None, with_distances=False):
     """ArborX::query(tree, space, predicates, indices, offsets[, policy]).
 
@@ -220,9 +262,10 @@ def query(tree, predicates, policy=None, space=None, with_distances=False):
     policy = policy or TraversalPolicy()
     s = _stream(space)
     h = ctypes.c_void_p()
+    prefix = getattr(tree, "_prefix", "abx_bvh")
     if isinstance(predicates, Intersects):
         check(
-            L.abx_bvh_query_intersects(
+            getattr(L, prefix + "_query_intersects")(
                 tree._h, s, predicates.kind, _ptr(predicates.data), len(predicates), policy._c(),
                 ctypes.byref(h),
             )
@@ -231,7 +274,7 @@ def query(tree, predicates, policy=None, space=None, with_distances=False):
         kt = predicates.k if isinstance(predicates.k, torch.Tensor) else None
         kv = 0 if kt is not None else predicates.k
         check(
-            L.abx_bvh_query_nearest(
+            getattr(L, prefix + "_query_nearest")(
                 tree._h, s, _ptr(predicates.data), len(predicates), _ptr(kt) if kt is not None else None,
                 kv, policy._c(), 1 if with_distances else 0, ctypes.byref(h),
             )

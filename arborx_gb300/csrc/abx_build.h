@@ -89,6 +89,13 @@ struct ForestView
   int nseg;
 };
 
+// Values of a brute-force index packed in input order like the Morton-ordered
+// leaves ({x, y, z, index}; two float4 per box).  A TreeView with null
+// tnodes is a brute-force index over such values: the query launchers then
+// test every predicate against every value.
+abx_status brute_pack(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
+                      float4 *d_values);
+
 // Spatial query modes.
 enum SpatialMode
 {

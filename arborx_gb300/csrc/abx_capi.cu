@@ -39,6 +39,11 @@ struct abx_forest : abx_bvh
 {
 };
 
+// Brute-force index: the values packed in input order (`sorted`), no nodes.
+struct abx_brute : abx_bvh
+{
+};
+
 struct abx_crs
 {
   int device = 0;
@@ -385,7 +390,7 @@ abx_status query_intersects(const abx_bvh *bvh, cudaStream_t s, abx_geometry kin
   }
   const ForestView *f = h_qoff ? &fv : nullptr;
   Scratch<uint32_t> perm;
-  if (policy.sort_predicates && nq > 1)
+  if (policy.sort_predicates && nq > 1 && bvh->tnodes)
   {
     abx_status st = sort_predicates(s, bvh, kind, d_predicates, nq, qoff.ptr, perm);
     if (st != ABX_SUCCESS)
@@ -497,7 +502,7 @@ abx_status query_nearest(const abx_bvh *bvh, cudaStream_t s, const float *d_quer
   }
   const ForestView *f = h_qoff ? &fv : nullptr;
   Scratch<uint32_t> perm;
-  if (policy.sort_predicates && nq > 1)
+  if (policy.sort_predicates && nq > 1 && bvh->tnodes)
   {
     abx_status st = sort_predicates(s, bvh, ABX_POINT, d_queries, nq, qoff.ptr, perm);
     if (st != ABX_SUCCESS)
@@ -943,6 +948,89 @@ abx_status abx_forest_query_nearest(const abx_forest *forest, void *stream,
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_query_nearest: null queries");
   return query_nearest(forest, as_stream(stream), d_queries, nq, h_query_offsets, d_k, k, policy,
                        with_distances, out);
+}
+
+abx_status abx_brute_create(void *stream, abx_geometry kind, const float *d_values, int64_t n,
+                            abx_brute **out)
+{
+  if (!out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_brute_create: null output handle");
+  *out = nullptr;
+  if (kind != ABX_POINT && kind != ABX_BOX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_brute_create: values must be points or boxes");
+  if (n < 0 || n >= (int64_t)INT32_MAX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_brute_create: size out of range [0, 2^31-1)");
+  if (n > 0 && !d_values)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_brute_create: null values");
+  device_state();
+  abx_brute *t = new (std::nothrow) abx_brute;
+  if (!t)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_brute_create: host allocation");
+  cudaGetDevice(&t->device);
+  t->stream = as_stream(stream);
+  t->kind = kind;
+  t->n = n;
+  cudaError_t e = cudaMallocHost(&t->h_bounds, 6 * sizeof(float));
+  if (e == cudaSuccess)
+    e = cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming);
+  abx_status st = e == cudaSuccess ? ABX_SUCCESS : fail_cuda(e, "abx_brute_create");
+  cudaStream_t s = t->stream;
+  if (st == ABX_SUCCESS)
+  {
+    const float empty[6] = {FLT_MAX, FLT_MAX, FLT_MAX, -FLT_MAX, -FLT_MAX, -FLT_MAX};
+    std::memcpy(t->h_bounds, empty, sizeof(empty));
+    if (dmalloc_n(&t->d_bounds, 6, s) != cudaSuccess ||
+        (n > 0 && dmalloc_n(&t->sorted, (size_t)n * (kind == ABX_BOX ? 2 : 1), s) != cudaSuccess))
+      st = fail(ABX_ERROR_OUT_OF_MEMORY, "abx_brute_create: device allocation");
+  }
+  if (st == ABX_SUCCESS && n > 0)
+  {
+    st = scene_bounds(s, kind, d_values, n, t->d_bounds);
+    if (st == ABX_SUCCESS)
+      st = brute_pack(s, kind, d_values, n, t->sorted);
+    if (st == ABX_SUCCESS &&
+        cudaMemcpyAsync(t->h_bounds, t->d_bounds, 6 * sizeof(float), cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess)
+      st = fail(ABX_ERROR_CUDA, "abx_brute_create: bounds copy");
+  }
+  if (st == ABX_SUCCESS && cudaEventRecord(t->ready, s) != cudaSuccess)
+    st = fail(ABX_ERROR_CUDA, "abx_brute_create: event");
+  if (st != ABX_SUCCESS)
+  {
+    cudaStreamSynchronize(s);
+    destroy_tree(t);
+    return st;
+  }
+  *out = t;
+  return ABX_SUCCESS;
+}
+
+abx_status abx_brute_destroy(abx_brute *brute)
+{
+  destroy_tree(brute);
+  return ABX_SUCCESS;
+}
+
+int64_t abx_brute_size(const abx_brute *brute) { return brute ? brute->n : 0; }
+
+abx_status abx_brute_bounds(const abx_brute *brute, float h_box[6])
+{
+  return abx_bvh_bounds(brute, h_box);
+}
+
+abx_status abx_brute_query_intersects(const abx_brute *brute, void *stream, abx_geometry kind,
+                                      const float *d_predicates, int64_t nq,
+                                      abx_traversal_policy policy, abx_crs **out)
+{
+  return abx_bvh_query_intersects(brute, stream, kind, d_predicates, nq, policy, out);
+}
+
+abx_status abx_brute_query_nearest(const abx_brute *brute, void *stream, const float *d_queries,
+                                   int64_t nq, const int32_t *d_k, int32_t k,
+                                   abx_traversal_policy policy, int32_t with_distances,
+                                   abx_crs **out)
+{
+  return abx_bvh_query_nearest(brute, stream, d_queries, nq, d_k, k, policy, with_distances, out);
 }
 
 int64_t abx_crs_num_queries(const abx_crs *crs) { return crs ? crs->nq : 0; }

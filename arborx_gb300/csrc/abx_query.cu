@@ -718,6 +718,242 @@ __global__ void k_knn_counts(int64_t n, ForestView f, const int32_t *__restrict_
 // Launchers
 // ---------------------------------------------------------------------------
 
+// ---------------------------------------------------------------------------
+// Brute force (ArborX_BruteForce.hpp:40-176, ArborX_BruteForceImpl.hpp:29-229):
+// every predicate against every value, values staged through shared memory
+// in tiles.  Values are packed like the Morton-ordered leaves, in input
+// order ({x, y, z, value} per point, two float4 per box).
+// ---------------------------------------------------------------------------
+
+constexpr int kBruteTile = 1024;
+
+template <int KIND>
+__device__ __forceinline__ void tile_leaf(const float4 *tile, int j, Box3 &b, int &v)
+{
+  const float4 u = tile[KIND == 1 ? 2 * j : j];
+  b.lo[0] = u.x;
+  b.lo[1] = u.y;
+  b.lo[2] = u.z;
+  if (KIND == 1)
+  {
+    const float4 w = tile[2 * j + 1];
+    b.hi[0] = w.x;
+    b.hi[1] = w.y;
+    b.hi[2] = w.z;
+  }
+  else
+  {
+    b.hi[0] = u.x;
+    b.hi[1] = u.y;
+    b.hi[2] = u.z;
+  }
+  v = __float_as_int(u.w);
+}
+
+// Load tile [t0, t0 + m) of the packed values into shared memory.
+template <int KIND>
+__device__ __forceinline__ int load_tile(float4 *tile, const float4 *__restrict__ values, int64_t n,
+                                         int64_t t0)
+{
+  constexpr int f4 = KIND == 1 ? 2 : 1;
+  const int m = (int)min((int64_t)kBruteTile, n - t0);
+  __syncthreads();
+  for (int j = threadIdx.x; j < m * f4; j += blockDim.x)
+    tile[j] = __ldg(values + t0 * f4 + j);
+  __syncthreads();
+  return m;
+}
+
+// Spatial: the matches of a predicate come out in ascending value order.
+template <int PRED, int MODE, int KIND>
+__global__ void __launch_bounds__(kQueryThreads)
+    k_brute_spatial(const float4 *__restrict__ values, int64_t n, const float *__restrict__ preds,
+                    int64_t nq, int32_t *__restrict__ counts, const int32_t *__restrict__ offsets,
+                    int32_t *__restrict__ out, int32_t buffer, unsigned *__restrict__ overflow)
+{
+  __shared__ float4 tile[kBruteTile * (KIND == 1 ? 2 : 1)];
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = q < nq;
+  const auto pred = PredOf<PRED>::load(preds, active ? q : 0);
+  int32_t *dst = nullptr;
+  if (MODE == kFill && active)
+    dst = out + __ldg(offsets + q);
+  if (MODE == kBuffered && active)
+    dst = out + q * (int64_t)buffer;
+  int32_t count = 0;
+  for (int64_t t0 = 0; t0 < n; t0 += kBruteTile)
+  {
+    const int m = load_tile<KIND>(tile, values, n, t0);
+    if (!active)
+      continue;
+    for (int j = 0; j < m; ++j)
+    {
+      Box3 b;
+      int v;
+      tile_leaf<KIND>(tile, j, b, v);
+      if (pred.template test_leaf<KIND>(b))
+      {
+        if (MODE == kFill || (MODE == kBuffered && count < buffer))
+          dst[count] = v;
+        ++count;
+      }
+    }
+  }
+  if (!active)
+    return;
+  if (MODE != kFill)
+    counts[q] = count;
+  if (MODE == kBuffered && count > buffer)
+    atomicOr(overflow, 1u);
+}
+
+// Nearest: the same sorted key list and (distance, index) rule as k_nearest,
+// so the results equal the tree's.
+template <int K, int KIND>
+__global__ void __launch_bounds__(kQueryThreads)
+    k_brute_nearest(const float4 *__restrict__ values, int64_t n, const float *__restrict__ queries,
+                    int64_t nq, const int32_t *__restrict__ kq, int32_t k_all,
+                    const int32_t *__restrict__ offsets, int32_t *__restrict__ offsets_out,
+                    int32_t *__restrict__ out_idx, float *__restrict__ out_dist)
+{
+  __shared__ float4 tile[kBruteTile * (KIND == 1 ? 2 : 1)];
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = t < nq;
+  KnnTask task{};
+  if (active)
+  {
+    QueryTree tree;
+    task = knn_task(t, n, ForestView{nullptr, nullptr, 1}, tree, nq, nullptr, kq, k_all,
+                    offsets, offsets_out);
+  }
+  const bool work = active && task.kk > 0;
+  uint64_t key[K];
+  const int first = K - (work ? task.k : 0);
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    key[j] = j < first ? 0ull : kKeyEmpty;
+  float thr = INFINITY;
+  float qx = 0, qy = 0, qz = 0;
+  if (work)
+  {
+    qx = __ldg(queries + 3 * task.q);
+    qy = __ldg(queries + 3 * task.q + 1);
+    qz = __ldg(queries + 3 * task.q + 2);
+  }
+  for (int64_t t0 = 0; t0 < n; t0 += kBruteTile)
+  {
+    const int m = load_tile<KIND>(tile, values, n, t0);
+    if (!work)
+      continue;
+    for (int j = 0; j < m; ++j)
+    {
+      Box3 b;
+      int v;
+      tile_leaf<KIND>(tile, j, b, v);
+      const float s = leaf_dist2<KIND>(qx, qy, qz, b);
+      if (s <= thr)
+      {
+        const uint64_t c = knn_key(__fsqrt_rn(s), v);
+        if (c < key[K - 1])
+        {
+          list_insert<K>(key, c);
+          if (key[K - 1] != kKeyEmpty)
+            thr = sq_threshold(key_dist(key[K - 1]));
+        }
+      }
+    }
+  }
+  if (!work)
+    return;
+  const int kk = task.kk;
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+  {
+    const int r = j - first;
+    if (r >= 0 && r < kk)
+    {
+      out_idx[task.base + r] = key_value(key[j]);
+      if (out_dist)
+        out_dist[task.base + r] = key_dist(key[j]);
+    }
+  }
+}
+
+// Nearest with k above 32: a binary heap per query in the output arrays.
+template <int KIND>
+__global__ void __launch_bounds__(kQueryThreads)
+    k_brute_nearest_large(const float4 *__restrict__ values, int64_t n,
+                          const float *__restrict__ queries, int64_t nq,
+                          const int32_t *__restrict__ kq, int32_t k_all,
+                          const int32_t *__restrict__ offsets, int32_t *__restrict__ offsets_out,
+                          int32_t *__restrict__ out_idx, float *__restrict__ out_dist)
+{
+  __shared__ float4 tile[kBruteTile * (KIND == 1 ? 2 : 1)];
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = t < nq;
+  KnnTask task{};
+  if (active)
+  {
+    QueryTree tree;
+    task = knn_task(t, n, ForestView{nullptr, nullptr, 1}, tree, nq, nullptr, kq, k_all,
+                    offsets, offsets_out);
+  }
+  const bool work = active && task.kk > 0;
+  const int kk = work ? task.kk : 0;
+  float *hd = work ? out_dist + task.base : nullptr;
+  int *hi = work ? out_idx + task.base : nullptr;
+  int size = 0;
+  float qx = 0, qy = 0, qz = 0;
+  if (work)
+  {
+    qx = __ldg(queries + 3 * task.q);
+    qy = __ldg(queries + 3 * task.q + 1);
+    qz = __ldg(queries + 3 * task.q + 2);
+  }
+  float thr = INFINITY;
+  for (int64_t t0 = 0; t0 < n; t0 += kBruteTile)
+  {
+    const int m = load_tile<KIND>(tile, values, n, t0);
+    if (!work)
+      continue;
+    for (int j = 0; j < m; ++j)
+    {
+      Box3 b;
+      int v;
+      tile_leaf<KIND>(tile, j, b, v);
+      const float s = leaf_dist2<KIND>(qx, qy, qz, b);
+      if (s > thr)
+        continue;
+      const float d = __fsqrt_rn(s);
+      if (size < kk)
+        heap_push(hd, hi, size, d, v);
+      else if (pair_lt(d, v, hd[0], hi[0]))
+        heap_sift_down(hd, hi, 0, size, d, v);
+      if (size == kk)
+        thr = sq_threshold(hd[0]);
+    }
+  }
+  if (!work)
+    return;
+  for (int len = size; len > 1; --len)
+  {
+    const float d0 = hd[0];
+    const int i0 = hi[0];
+    heap_sift_down(hd, hi, 0, len - 1, hd[len - 1], hi[len - 1]);
+    hd[len - 1] = d0;
+    hi[len - 1] = i0;
+  }
+}
+
+// Pack values in input order: {x, y, z, index} (two float4 per box).
+template <int KIND>
+__global__ void k_brute_pack(const float *__restrict__ g, int64_t n, float4 *__restrict__ values)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    SortedLeaf<KIND>::store(values, i, load_leaf_box<KIND>(g, i), (int)i);
+}
+
 template <int PRED, int KIND>
 abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, ForestView const &f,
                             const float *d_preds,
@@ -734,12 +970,25 @@ abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, ForestView const 
                                                             nq, d_perm, d_counts, d_offsets,  \
                                                             d_out, buffer, bucket, d_overflow, \
                                                             err)
-  if (mode == kCount)
+#define ABX_BRUTE(M)                                                                         \
+  k_brute_spatial<PRED, M, KIND><<<blocks, kQueryThreads, 0, s>>>(                               \
+      t.sorted, t.n, d_preds, nq, d_counts, d_offsets, d_out, buffer, d_overflow)
+  if (!t.tnodes) // brute force: every predicate against every value
+  {
+    if (mode == kCount)
+      ABX_BRUTE(kCount);
+    else if (mode == kFill)
+      ABX_BRUTE(kFill);
+    else
+      ABX_BRUTE(kBuffered);
+  }
+  else if (mode == kCount)
     ABX_SPATIAL(kCount);
   else if (mode == kFill)
     ABX_SPATIAL(kFill);
   else
     ABX_SPATIAL(kBuffered);
+#undef ABX_BRUTE
 #undef ABX_SPATIAL
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
@@ -755,7 +1004,10 @@ abx_status nearest_k(cudaStream_t s, TreeView const &t, ForestView const &f,
   const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
   const int bucket =
       std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
-  if (bucket >= 2)
+  if (!t.tnodes) // brute force
+    k_brute_nearest<K, KIND><<<blocks, kQueryThreads, 0, s>>>(
+        t.sorted, t.n, d_queries, nq, d_k, k, d_offsets, d_offsets_out, d_idx, d_dist);
+  else if (bucket >= 2)
     k_nearest<K, KIND, true><<<blocks, kQueryThreads, 0, s>>>(
         t.tnodes, t.sorted, t.n, f, d_queries, nq, d_perm, d_k, k, d_offsets, d_offsets_out, d_idx,
         d_dist, bucket, err);
@@ -794,6 +1046,10 @@ abx_status nearest_dispatch(cudaStream_t s, TreeView const &t, ForestView const 
   const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
   const int bucket =
       std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
+  if (!t.tnodes)
+    k_brute_nearest_large<KIND><<<blocks, kQueryThreads, 0, s>>>(
+        t.sorted, t.n, d_queries, nq, d_k, k, d_offsets, d_offsets_out, d_idx, d_dist);
+  else
   k_nearest_large<KIND><<<blocks, kQueryThreads, 0, s>>>(t.tnodes, t.sorted, t.n, f, d_queries, nq,
                                                          d_perm, d_k, k, d_offsets,
                                                          d_offsets_out, d_idx, d_dist, bucket,
@@ -826,6 +1082,20 @@ abx_status launch_spatial(cudaStream_t s, TreeView const &t, ForestView const *f
                       : spatial_dispatch<ABX_BOX, 0>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
                                                      d_offsets, d_out, buffer, d_overflow);
   return fail(ABX_ERROR_INVALID_ARGUMENT, "intersects predicates must be spheres or boxes");
+}
+
+abx_status brute_pack(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
+                      float4 *d_values)
+{
+  if (n <= 0)
+    return ABX_SUCCESS;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  if (kind == ABX_BOX)
+    k_brute_pack<1><<<blocks, 256, 0, s>>>(d_g, n, d_values);
+  else
+    k_brute_pack<0><<<blocks, 256, 0, s>>>(d_g, n, d_values);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
 }
 
 abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int32_t buffer,

@@ -52,6 +52,7 @@ typedef enum abx_status
 typedef struct abx_bvh abx_bvh; /* opaque tree                                */
 typedef struct abx_crs abx_crs; /* opaque CRS result (offsets + indices)      */
 typedef struct abx_forest abx_forest; /* opaque batch of independent trees    */
+typedef struct abx_brute abx_brute;   /* opaque brute-force index             */
 
 /* Geometry of values and predicates, float32, array-of-structures:
  *   POINT  x y z                 (12 bytes)   ArborX::Point<3>
@@ -261,6 +262,31 @@ ABX_API abx_status abx_forest_query_nearest(const abx_forest *forest,
                                             abx_traversal_policy policy,
                                             int32_t with_distances,
                                             abx_crs **out);
+
+/* ---------------------------------------------------------------------- */
+/* Brute force (src/spatial/ArborX_BruteForce.hpp:40-176)                  */
+/* ---------------------------------------------------------------------- */
+/* BruteForce(space, values): every predicate is tested against every value
+ * (ArborX_BruteForceImpl.hpp:29-229), values staged through shared memory.
+ * Same predicates, policies and CRS output as the tree queries:
+ * intersects returns each query's matches in ascending value order (the
+ * reference's order is that of its atomic inserts); nearest returns exactly
+ * what abx_bvh_query_nearest returns on a tree of the same values (k smallest
+ * (distance, index), ascending).  Predicate sorting is a no-op here. */
+ABX_API abx_status abx_brute_create(void *stream, abx_geometry kind, const float *d_values,
+                                    int64_t n, abx_brute **out);
+ABX_API abx_status abx_brute_destroy(abx_brute *brute);
+ABX_API int64_t abx_brute_size(const abx_brute *brute);
+ABX_API abx_status abx_brute_bounds(const abx_brute *brute, float h_box[6]);
+ABX_API abx_status abx_brute_query_intersects(const abx_brute *brute, void *stream,
+                                              abx_geometry kind, const float *d_predicates,
+                                              int64_t nq, abx_traversal_policy policy,
+                                              abx_crs **out);
+ABX_API abx_status abx_brute_query_nearest(const abx_brute *brute, void *stream,
+                                           const float *d_queries, int64_t nq,
+                                           const int32_t *d_k, int32_t k,
+                                           abx_traversal_policy policy, int32_t with_distances,
+                                           abx_crs **out);
 
 /* ---------------------------------------------------------------------- */
 /* Serving: a request loop over trees resident in HBM                      */

@@ -1,0 +1,77 @@
+"""BruteForce (src/spatial/ArborX_BruteForce.hpp:40-176): exact all-pairs
+queries.  Nearest results equal the tree's and the oracle's bit for bit;
+intersects results equal the oracle's brute force in ascending value order."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import oracle as o
+from tests.helpers import uniform_points
+
+pytestmark = pytest.mark.gpu
+
+
+def cuda(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def bits(a):
+    return np.asarray(a, np.float32).view(np.int32)
+
+
+@pytest.mark.parametrize("k", [1, 5, 16, 32, 40])
+def test_brute_nearest_equals_tree_and_oracle(ax, k):
+    p = uniform_points(3000, 50)
+    p[100:140] = p[100]  # exact ties
+    q = uniform_points(777, 51)
+    bf = ax.BruteForce(cuda(p))
+    bvh = ax.BoundingVolumeHierarchy(cuda(p))
+    bi, bo, bd = ax.query(bf, ax.nearest(cuda(q), k), with_distances=True)
+    ti, to, td = ax.query(bvh, ax.nearest(cuda(q), k), with_distances=True)
+    assert np.array_equal(bo.cpu().numpy(), to.cpu().numpy())
+    assert np.array_equal(bi.cpu().numpy(), ti.cpu().numpy())
+    assert np.array_equal(bits(bd.cpu().numpy()), bits(td.cpu().numpy()))
+    ri, rd = o.knn_brute(p, q, k)
+    assert np.array_equal(bi.cpu().numpy(), ri.ravel())
+    assert np.array_equal(bits(bd.cpu().numpy()), bits(rd.ravel()))
+
+
+def test_brute_nearest_per_query_k_and_boxes(ax):
+    rng = np.random.default_rng(3)
+    lo = uniform_points(2500, 52)
+    b = np.concatenate([lo, lo + 0.01 * uniform_points(2500, 53)], axis=1)
+    q = uniform_points(500, 54)
+    kq = rng.integers(-1, 50, 500).astype(np.int32)
+    bf = ax.BruteForce(cuda(b), kind=1)
+    bvh = ax.BoundingVolumeHierarchy(cuda(b), kind=1)
+    a = ax.query(bf, ax.nearest(cuda(q), cuda(kq)))
+    t = ax.query(bvh, ax.nearest(cuda(q), cuda(kq)))
+    assert all(np.array_equal(x.cpu().numpy(), y.cpu().numpy()) for x, y in zip(a, t))
+
+
+@pytest.mark.parametrize("buffer", [0, 3, -1000])
+def test_brute_spatial_equals_oracle(ax, buffer):
+    p = uniform_points(5000, 55)
+    rng = np.random.default_rng(4)
+    sph = np.concatenate([uniform_points(1000, 56), rng.uniform(0, 0.08, (1000, 1))], axis=1).astype(np.float32)
+    bf = ax.BruteForce(cuda(p))
+    pol = ax.TraversalPolicy().setBufferSize(buffer)
+    i, off = ax.query(bf, ax.intersects(cuda(sph)), pol)
+    ro, ri = o.spatial_brute(p, o.KIND_SPHERE, sph)
+    assert np.array_equal(off.cpu().numpy(), ro)
+    assert np.array_equal(i.cpu().numpy(), ri)  # ascending value order
+    boxes = np.concatenate([uniform_points(300, 57), uniform_points(300, 57) + 0.05], axis=1)
+    i, off = ax.query(bf, ax.intersects(cuda(boxes)))
+    ro, ri = o.spatial_brute(p, o.KIND_BOX, boxes)
+    assert np.array_equal(off.cpu().numpy(), ro) and np.array_equal(i.cpu().numpy(), ri)
+
+
+def test_brute_empty_and_bounds(ax):
+    e = ax.BruteForce(torch.zeros((0, 3), device="cuda"))
+    assert e.empty()
+    i, off = ax.query(e, ax.nearest(cuda(uniform_points(4, 1)), 3))
+    assert off.cpu().numpy().tolist() == [0] * 5 and i.numel() == 0
+    p = uniform_points(100, 2)
+    bf = ax.BruteForce(cuda(p))
+    assert np.array_equal(bits(bf.bounds()), bits(np.concatenate([p.min(0), p.max(0)])))
