@@ -52,8 +52,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--n", type=int, default=N_POINTS)
-    ap.add_argument("--nq", type=int, default=N_QUERIES)
+    ap.add_argument("--points", "--n", dest="n", type=int, default=N_POINTS)
+    ap.add_argument("--queries", "--nq", dest="nq", type=int, default=N_QUERIES)
     ap.add_argument("--k", type=int, default=K)
     ap.add_argument("--cpu-sample", type=int, default=1_000_000,
                     help="queries timed per CPU step (scaled to --nq)")
@@ -72,10 +72,9 @@ def parse():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    from arborx_gb300.replicas import env
+
+    return env()
 
 
 def clustered(n, seed_pick, seed_offset):
@@ -94,8 +93,10 @@ def clustered(n, seed_pick, seed_offset):
 def make_inputs(n, nq, rank, dist="uniform"):
     if dist == "clustered":
         return clustered(n, 8 + 1000 * rank, 9 + 1000 * rank), clustered(nq, 10 + 1000 * rank, 11 + 1000 * rank)
-    rng_p = np.random.default_rng(3 + 1000 * rank)
-    rng_q = np.random.default_rng(12 + 1000 * rank)
+    from arborx_gb300.replicas import replica_seed
+
+    rng_p = np.random.default_rng(replica_seed(3, rank))
+    rng_q = np.random.default_rng(replica_seed(12, rank))
     return rng_p.random((n, 3), dtype=np.float32), rng_q.random((nq, 3), dtype=np.float32)
 
 
@@ -303,12 +304,12 @@ def config_of(args):
 
 def run_gpu(args):
     import torch
-    import torch.distributed as dist
+
+    from arborx_gb300.replicas import Replicas, whole_job_rate
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
-    if world > 1:
-        dist.init_process_group("nccl")
+    group = Replicas("nccl", device=local)
 
     import arborx_gb300 as ax
     from arborx_gb300 import _lib
@@ -325,10 +326,7 @@ def run_gpu(args):
     stream = torch.cuda.current_stream()
 
     def barrier():
-        torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
+        group.barrier()
 
     def step():
         bvh = ax.BoundingVolumeHierarchy(points)
@@ -336,11 +334,7 @@ def run_gpu(args):
         return bvh, ind, off
 
     def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return group.max(x)
 
     for _ in range(args.warmup):
         keep = step()
@@ -452,7 +446,7 @@ def run_gpu(args):
         "kernel_ms": nearest_ms,
     }
     build_achieved = BUILD_BYTES_PER_POINT * args.n / (build_ms * 1e-3) / 1e9
-    value = args.nq * world / (ms_step * 1e-3)
+    value = whole_job_rate(args.nq, ms_step * 1e-3, world)
 
     line = None
     if rank == 0:
@@ -494,9 +488,8 @@ def run_gpu(args):
             cpu = cpu_baseline(points_np, queries_np, args.k, args.cpu_sample)
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.barrier()
-        dist.destroy_process_group()
+    group.barrier()
+    group.close()
 
 
 def run_case(args):
