@@ -514,6 +514,25 @@ __global__ void __launch_bounds__(kQueryThreads)
     if (!found)
       break;
   }
+  if (K % 4 == 0 && first == 0 && task.kk == K && (task.base & 3) == 0)
+  {
+    // a full list at a 16-byte aligned offset: vector stores, so each
+    // query's results leave as whole sectors
+    int4 *oi = reinterpret_cast<int4 *>(out_idx + task.base);
+#pragma unroll
+    for (int j = 0; j < K; j += 4)
+      oi[j / 4] = make_int4(key_value(key[j]), key_value(key[j + 1]), key_value(key[j + 2]),
+                            key_value(key[j + 3]));
+    if (out_dist)
+    {
+      float4 *od = reinterpret_cast<float4 *>(out_dist + task.base);
+#pragma unroll
+      for (int j = 0; j < K; j += 4)
+        od[j / 4] = make_float4(key_dist(key[j]), key_dist(key[j + 1]), key_dist(key[j + 2]),
+                                key_dist(key[j + 3]));
+    }
+    return;
+  }
 #pragma unroll
   for (int j = 0; j < K; ++j)
   {

@@ -284,3 +284,4 @@ def _check_variant_results(ax, bvh, ref, q):
     ind, off = ax.query(bvh, ax.intersects(cuda(boxes)))
     assert np.array_equal(host(off), roff) and np.array_equal(host(ind), rind)
     assert ax.device_errors() == 0
+
