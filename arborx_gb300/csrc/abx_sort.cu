@@ -320,31 +320,58 @@ __device__ __forceinline__ void run_bounds(const K *__restrict__ keys, int64_t n
 
 // Keys sorted (stably) by their top bits: place every key of a run of at
 // most kRunMax equal top-bit keys at its rank by (key, position), which is the
-// stable order; keys of longer runs are copied in place and counted.
+// stable order; keys of longer runs are copied in place and counted.  A CTA
+// stages its keys with a halo of kFixHalo on each side in shared memory,
+// with the top bits as 32-bit words (fewer than 32 bits remain above any
+// shift used here) and sentinels past both ends of the array.
+constexpr int kFixThreads = 256;
+constexpr int kFixHalo = kRunMax + 2;
+
 template <class K>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kFixThreads)
     k_run_fixup(const K *__restrict__ kin, const uint32_t *__restrict__ vin, K *__restrict__ kout,
                 uint32_t *__restrict__ vout, int64_t n, int shift,
                 unsigned long long *__restrict__ long_count)
 {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr int kSpan = kFixThreads + 2 * kFixHalo;
+  __shared__ K s_key[kSpan];
+  __shared__ uint32_t s_top[kSpan];
+  const int64_t b = (int64_t)blockIdx.x * kFixThreads;
+  for (int j = threadIdx.x; j < kSpan; j += kFixThreads)
+  {
+    const int64_t g = b - kFixHalo + j;
+    const bool in = g >= 0 && g < n;
+    const K k = in ? kin[g] : (K)0;
+    s_key[j] = k;
+    // tops are below 2^24; the two sentinels differ from them and each other
+    s_top[j] = in ? (uint32_t)(k >> shift) : (g < 0 ? 0xffffffffu : 0xfffffffeu);
+  }
+  __syncthreads();
+  const int64_t i = b + threadIdx.x;
   bool is_long = false;
   if (i < n)
   {
-    const K k = kin[i];
-    int64_t a, b;
-    run_bounds(kin, n, i, (K)(k >> shift), shift, a, b);
+    const int li = threadIdx.x + kFixHalo;
+    const uint32_t top = s_top[li];
+    int a = li;
+    while (li - a <= kRunMax && s_top[a - 1] == top)
+      --a;
+    int e = li + 1;
+    while (e - a <= kRunMax && s_top[e] == top)
+      ++e;
+    const K k = s_key[li];
     int64_t r = i;
-    if (b - a > kRunMax)
+    if (e - a > kRunMax)
       is_long = true;
     else
     {
-      r = a;
-      for (int64_t j = a; j < b; ++j)
+      int rank = a;
+      for (int j = a; j < e; ++j)
       {
-        const K kj = kin[j];
-        r += (kj < k) || (kj == k && j < i);
+        const K kj = s_key[j];
+        rank += (kj < k) || (kj == k && j < li);
       }
+      r = b - kFixHalo + rank;
     }
     kout[r] = k;
     vout[r] = vin[i];
@@ -519,7 +546,8 @@ abx_status radix_sort_hybrid(cudaStream_t s, K *d_keys, uint32_t *d_vals,
   ABX_CUDA_TRY(long_count.alloc(1, s));
   ABX_CUDA_TRY(cudaMemsetAsync(long_count.ptr, 0, sizeof(unsigned long long), s));
   const unsigned blocks = (unsigned)((n + 255) / 256);
-  k_run_fixup<K><<<blocks, 256, 0, s>>>(kin, vin, kout, vout, n, shift, long_count.ptr);
+  k_run_fixup<K><<<(unsigned)((n + kFixThreads - 1) / kFixThreads), kFixThreads, 0, s>>>(
+      kin, vin, kout, vout, n, shift, long_count.ptr);
   ABX_CUDA_TRY(cudaGetLastError());
   ++launches;
   unsigned long long m = 0;
@@ -579,6 +607,8 @@ abx_status radix_sort_impl(cudaStream_t s, K *d_keys, uint32_t *d_vals,
     return fail(ABX_ERROR_INVALID_ARGUMENT, "radix sort: bad number of passes");
   if (top < 0 || top >= num_passes)
     top = 0;
+  // the fix-up keeps the top bits in 32-bit words with two reserved values
+  top = std::min(top, 3);
   StageScope scope(s, sizeof(K) == 8 ? "sort64" : "sort32", 0);
   int launches = 0;
   abx_status st = top > 0
