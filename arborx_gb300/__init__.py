@@ -31,6 +31,7 @@ from .bvh import (  # noqa: F401
     morton64,
     nearest,
     query,
+    query_nearest_into,
     scene_bounds,
     sort_u32,
     sort_u64,

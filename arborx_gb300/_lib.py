@@ -58,6 +58,11 @@ class ServerStatisticsC(ctypes.Structure):
 REQ_NEAREST = 0
 REQ_INTERSECTS = 1
 
+class ValuesC(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("value_stride", ctypes.c_int64),
+                ("coord_stride", ctypes.c_int64)]
+
+
 SIGNATURES = {
     "abx_status_string": (ctypes.c_char_p, [_STATUS]),
     "abx_last_error": (ctypes.c_char_p, []),
@@ -69,6 +74,7 @@ SIGNATURES = {
     "abx_profiling_stage": (_STATUS, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(_I64)]),
     "abx_profiling_reset": (_STATUS, []),
     "abx_bvh_create": (_STATUS, [_P, ctypes.c_int, _P, _I64, ctypes.POINTER(_P)]),
+    "abx_bvh_create_strided": (_STATUS, [_P, ctypes.c_int, ValuesC, _I64, ctypes.POINTER(_P)]),
     "abx_bvh_destroy": (_STATUS, [_P]),
     "abx_bvh_size": (_I64, [_P]),
     "abx_bvh_bounds": (_STATUS, [_P, _P]),
@@ -117,6 +123,9 @@ SIGNATURES = {
     "abx_server_result": (_STATUS, [_P, _I64, _P, _P, _P]),
     "abx_server_stats": (_STATUS, [_P, ctypes.POINTER(ServerStatisticsC)]),
     "abx_server_reset_stats": (_STATUS, [_P]),
+    "abx_bvh_query_nearest_into": (
+        _STATUS, [_P, _P, _P, _I64, _I32, TraversalPolicyC, _P, _P, _P],
+    ),
     "abx_crs_num_queries": (_I64, [_P]),
     "abx_crs_num_results": (_I64, [_P]),
     "abx_crs_offsets": (_P, [_P]),

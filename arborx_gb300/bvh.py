@@ -168,9 +168,18 @@ class BoundingVolumeHierarchy:
             if kind is None:
                 raise ValueError("values must have 3 (point) or 6 (box) columns")
         self.kind = kind
-        v = _as_rows(values, 3 if kind == POINT else 6, "values")
         self._stream = _stream(space)
-        check(L.abx_bvh_create(self._stream, kind, _ptr(v), v.shape[0], ctypes.byref(self._h)))
+        cols = 3 if kind == POINT else 6
+        if (isinstance(values, torch.Tensor) and values.is_cuda and values.dtype == torch.float32
+                and values.dim() == 2 and values.shape[1] == cols and not values.is_contiguous()):
+            # any layout (access traits): read through the tensor's strides
+            v = values
+            vals = _lib.ValuesC(v.data_ptr(), v.stride(0), v.stride(1))
+            check(L.abx_bvh_create_strided(self._stream, kind, vals, v.shape[0],
+                                           ctypes.byref(self._h)))
+        else:
+            v = _as_rows(values, cols, "values")
+            check(L.abx_bvh_create(self._stream, kind, _ptr(v), v.shape[0], ctypes.byref(self._h)))
         self._values = v  # kept until the build has consumed it
 
     def __del__(self):
@@ -282,6 +291,21 @@ def query(tree, predicates, policy=None, space=None, with_distances=False):
     else:
         raise TypeError("predicates must be Intersects or Nearest")
     return _crs_result(h, isinstance(predicates, Nearest) and with_distances)
+
+
+def query_nearest_into(tree, queries, k, offsets, indices, distances=None, policy=None,
+                       space=None):
+    """nearest(point, k) into preallocated int32 offsets [nq + 1] and indices
+    [nq * min(k, size)] (and float32 distances) with no host synchronisation:
+    the call can be captured in a CUDA graph (torch.cuda.graph) and replayed."""
+    policy = policy or TraversalPolicy()
+    q = _as_rows(queries, 3, "queries")
+    for t, name in ((offsets, "offsets"), (indices, "indices")):
+        if not (isinstance(t, torch.Tensor) and t.is_cuda and t.dtype == torch.int32 and t.is_contiguous()):
+            raise TypeError("%s must be a contiguous int32 CUDA tensor" % name)
+    check(_lib.load().abx_bvh_query_nearest_into(
+        tree._h, _stream(space), _ptr(q), q.shape[0], int(k), policy._c(), _ptr(offsets),
+        _ptr(indices), _ptr(distances) if distances is not None else None))
 
 
 def _crs_result(h, with_distances):

@@ -261,6 +261,17 @@ int grid_for(int64_t n, int threads, int per_sm)
   return (int)std::max<int64_t>(1, std::min<int64_t>(b, (int64_t)ds.num_sms * per_sm));
 }
 
+// Row-major copy of values read through strides (access traits).
+__global__ void k_pack_strided(const float *__restrict__ data, int64_t value_stride,
+                               int64_t coord_stride, int64_t n, int cols, float *__restrict__ out)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n)
+    return;
+  for (int d = 0; d < cols; ++d)
+    out[i * cols + d] = __ldg(data + i * value_stride + d * coord_stride);
+}
+
 } // namespace
 
 abx_status scene_bounds(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
@@ -315,6 +326,17 @@ abx_status single_leaf(cudaStream_t s, abx_geometry kind, const float *d_g,
     k_single_leaf<0><<<1, 1, 0, s>>>(d_g, d_leaves, d_tnodes, d_sorted, d_bounds);
   else
     k_single_leaf<1><<<1, 1, 0, s>>>(d_g, d_leaves, d_tnodes, d_sorted, d_bounds);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
+
+abx_status pack_strided(cudaStream_t s, const float *d_data, int64_t value_stride,
+                        int64_t coord_stride, int64_t n, int cols, float *d_out)
+{
+  if (n <= 0)
+    return ABX_SUCCESS;
+  k_pack_strided<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_data, value_stride, coord_stride,
+                                                              n, cols, d_out);
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
 }

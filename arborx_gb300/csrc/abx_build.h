@@ -89,6 +89,10 @@ struct ForestView
   int nseg;
 };
 
+// Row-major copy (cols floats per value) of values read through strides.
+abx_status pack_strided(cudaStream_t s, const float *d_data, int64_t value_stride,
+                        int64_t coord_stride, int64_t n, int cols, float *d_out);
+
 // Values of a brute-force index packed in input order like the Morton-ordered
 // leaves ({x, y, z, index}; two float4 per box).  A TreeView with null
 // tnodes is a brute-force index over such values: the query launchers then

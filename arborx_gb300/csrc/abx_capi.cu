@@ -66,6 +66,12 @@ constexpr int kMaxDevices = 64;
 DeviceState g_states[kMaxDevices];
 } // namespace
 
+bool stream_capturing(cudaStream_t s)
+{
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &st) == cudaSuccess && st == cudaStreamCaptureStatusActive;
+}
+
 DeviceState &device_state()
 {
   int dev = 0;
@@ -92,6 +98,7 @@ DeviceState &device_state()
     }
     st.num_sms = sms > 0 ? sms : 1;
     st.d_error = err;
+    init_sort_kernels();
     st.device = dev;
   }
   return st;
@@ -324,8 +331,9 @@ abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
   ABX_CUDA_TRY(hist.alloc(4 * 256, s));
   ABX_CUDA_TRY(cudaMemsetAsync(hist.ptr, 0, 4 * 256 * sizeof(uint32_t), s));
   ABX_TRY(morton32_codes(s, kind, d_preds, nq, t->d_bounds, codes.ptr, hist.ptr));
+  // the hybrid sort reads a count back to the host: not while capturing
   ABX_TRY(radix_sort_u32(s, codes.ptr, perm.ptr, nullptr, nq, 4, hist.ptr,
-                         hybrid_top_passes(nq, 4)));
+                         stream_capturing(s) ? 0 : hybrid_top_passes(nq, 4)));
   return ABX_SUCCESS;
 }
 
@@ -712,6 +720,32 @@ abx_status abx_bvh_create(void *stream, abx_geometry kind, const float *d_values
   return ABX_SUCCESS;
 }
 
+abx_status abx_bvh_create_strided(void *stream, abx_geometry kind, abx_values values, int64_t n,
+                                  abx_bvh **out)
+{
+  if (!out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: null output handle");
+  *out = nullptr;
+  if (kind != ABX_POINT && kind != ABX_BOX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: points or boxes");
+  if (n < 0 || n >= (int64_t)INT32_MAX || values.value_stride < 0 || values.coord_stride < 0)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: bad size or strides");
+  if (n > 0 && !values.data)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: null values");
+  const int cols = kind == ABX_BOX ? 6 : 3;
+  if (values.value_stride == cols && values.coord_stride == 1)
+    return abx_bvh_create(stream, kind, values.data, n, out);
+  cudaStream_t s = as_stream(stream);
+  device_state();
+  Scratch<float> packed;
+  ABX_CUDA_TRY(packed.alloc((size_t)std::max<int64_t>(n, 1) * cols, s));
+  ABX_TRY(pack_strided(s, values.data, values.value_stride, values.coord_stride, n, cols,
+                       packed.ptr));
+  // the build reads the packed rows on the same stream; the scratch is
+  // released stream-ordered after it
+  return abx_bvh_create(stream, kind, packed.ptr, n, out);
+}
+
 abx_status abx_bvh_destroy(abx_bvh *bvh)
 {
   destroy_tree(bvh);
@@ -793,6 +827,46 @@ abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream, const float *
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: null queries");
   return query_nearest(bvh, as_stream(stream), d_queries, nq, nullptr, d_k, k, policy,
                        with_distances, out);
+}
+
+abx_status abx_bvh_query_nearest_into(const abx_bvh *bvh, void *stream, const float *d_queries,
+                                      int64_t nq, int32_t k, abx_traversal_policy policy,
+                                      int32_t *d_offsets, int32_t *d_indices, float *d_distances)
+{
+  if (!bvh || !d_offsets)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: null argument");
+  if (bvh->d_off)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: a forest handle");
+  if (nq < 0 || nq >= (int64_t)INT32_MAX || (nq > 0 && !d_queries))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: bad queries");
+  cudaStream_t s = as_stream(stream);
+  device_state();
+  if (!stream_capturing(s))
+    ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+  if (k < 0)
+    k = 0;
+  const int64_t kk = std::min<int64_t>(k, bvh->n);
+  if (kk * nq >= (int64_t)INT32_MAX)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: too many results");
+  if (nq > 0 && kk > 0 && !d_indices)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: null indices");
+  if (nq == 0 || kk == 0)
+  {
+    ABX_CUDA_TRY(cudaMemsetAsync(d_offsets, 0, (nq + 1) * sizeof(int32_t), s));
+    return ABX_SUCCESS;
+  }
+  Scratch<uint32_t> perm;
+  if (policy.sort_predicates && nq > 1 && bvh->tnodes)
+    ABX_TRY(sort_predicates(s, bvh, ABX_POINT, d_queries, nq, nullptr, perm));
+  Scratch<float> dist_tmp;
+  float *dist = d_distances;
+  if (!dist && k > 32)
+  {
+    ABX_CUDA_TRY(dist_tmp.alloc((size_t)(kk * nq), s));
+    dist = dist_tmp.ptr;
+  }
+  return launch_nearest(s, view_of(bvh), nullptr, d_queries, nq, perm.ptr, nullptr, k, k, nullptr,
+                        d_offsets, d_indices, dist);
 }
 
 abx_status abx_forest_create(void *stream, abx_geometry kind, const float *d_values,

@@ -125,6 +125,12 @@ abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,
                           const uint32_t *d_hist, int top_passes = 0);
 
+// Kernel attributes of the sort, set once per device by device_state().
+abx_status init_sort_kernels();
+
+// True when s is capturing a CUDA graph (no host synchronisation allowed).
+bool stream_capturing(cudaStream_t s);
+
 // Number of top passes of the hybrid sort for n keys of num_passes digits
 // (0 = plain LSD).
 int hybrid_top_passes(int64_t n, int num_passes);

@@ -470,13 +470,6 @@ abx_status sort_passes(cudaStream_t s, K *d_keys, uint32_t *d_vals, const uint32
   ++launches;
 
   const size_t smem = sizeof(PassSmem<K>);
-  static bool attr_set = false;
-  if (!attr_set)
-  {
-    ABX_CUDA_TRY(cudaFuncSetAttribute(k_onesweep<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem));
-    attr_set = true;
-  }
 
   const K *kin = d_keys;
   const uint32_t *vin = d_vals_in;
@@ -746,6 +739,19 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int32_t *__re
 }
 
 } // namespace
+
+abx_status init_sort_kernels()
+{
+  // dynamic shared memory of the onesweep passes (above the 48 KB default);
+  // set once per device, outside any stream capture
+  ABX_CUDA_TRY(cudaFuncSetAttribute(k_onesweep<uint64_t>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(PassSmem<uint64_t>)));
+  ABX_CUDA_TRY(cudaFuncSetAttribute(k_onesweep<uint32_t>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)sizeof(PassSmem<uint32_t>)));
+  return ABX_SUCCESS;
+}
 
 abx_status radix_sort_u64(cudaStream_t s, uint64_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,

@@ -135,6 +135,23 @@ ABX_API abx_status abx_tuning_reset(void);
 ABX_API abx_status abx_bvh_create(void *stream, abx_geometry kind,
                           const float *d_values, int64_t n, abx_bvh **out);
 
+/* Values through access traits (ArborX_AccessTraits.hpp:36-76: a rank-2
+ * View of n rows, any layout): coordinate d of value i is
+ * data[i * value_stride + d * coord_stride], d < 3 for points, < 6 for boxes
+ * (min x y z, max x y z).  Row-major n x 3 is (3, 1), column-major (SoA,
+ * Kokkos::LayoutLeft) is (1, n), padded float4 rows are (4, 1).  Strides are
+ * in floats and may be any non-negative values; the tree is the one
+ * abx_bvh_create builds from the same values packed row-major. */
+typedef struct abx_values
+{
+  const float *data;
+  int64_t value_stride;
+  int64_t coord_stride;
+} abx_values;
+
+ABX_API abx_status abx_bvh_create_strided(void *stream, abx_geometry kind, abx_values values,
+                                          int64_t n, abx_bvh **out);
+
 /* Destroy a tree (frees stream-ordered on the stream it was built on). */
 ABX_API abx_status abx_bvh_destroy(abx_bvh *bvh);
 
@@ -348,6 +365,18 @@ ABX_API abx_status abx_server_result(abx_server *srv, int64_t ticket, int32_t *h
                                      int32_t *h_indices, float *h_distances);
 ABX_API abx_status abx_server_stats(abx_server *srv, abx_server_statistics *out);
 ABX_API abx_status abx_server_reset_stats(abx_server *srv);
+
+/* nearest(point, k) with one k for all queries into caller-provided device
+ * arrays and no host synchronisation, so that the call can be captured in a
+ * CUDA graph and replayed (the queries' contents may change between
+ * replays).  d_offsets (nq + 1), d_indices (nq * min(k, size())) and, if not
+ * NULL, d_distances receive what abx_bvh_query_nearest returns.  While the
+ * stream is capturing, the tree's build must already have completed (for
+ * instance abx_bvh_bounds returned): the call does not wait on it then. */
+ABX_API abx_status abx_bvh_query_nearest_into(const abx_bvh *bvh, void *stream,
+                                              const float *d_queries, int64_t nq, int32_t k,
+                                              abx_traversal_policy policy, int32_t *d_offsets,
+                                              int32_t *d_indices, float *d_distances);
 
 /* Accessors of a CRS result: device offsets (nq + 1), device indices
  * (num_results), device distances (nearest only, else NULL). */

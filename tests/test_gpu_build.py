@@ -208,3 +208,23 @@ def test_sort_u32_hybrid(ax):
         ref = np.argsort(keys, kind="stable").astype(np.uint32)
         assert np.array_equal(perm, ref)
         assert np.array_equal(t.cpu().numpy().view(np.uint32), keys[ref])
+
+
+def test_strided_values_build_the_same_tree(ax):
+    """Access traits: column-major (SoA), padded float4 and sliced views build
+    exactly the tree of the row-major copy (ArborX_AccessTraits.hpp:36-76)."""
+    p = uniform_points(50000, 77)
+    ref = [x.cpu().numpy() for x in ax.BoundingVolumeHierarchy(cuda(p)).export_nodes()]
+    soa = cuda(np.ascontiguousarray(p.T)).t()            # strides (1, n)
+    pad = cuda(np.concatenate([p, np.zeros((p.shape[0], 1), np.float32)], axis=1))[:, :3]  # (4, 1)
+    big = cuda(np.repeat(p, 2, axis=0))[::2]             # (6, 1)
+    for v in (soa, pad, big):
+        assert not v.is_contiguous()
+        got = [x.cpu().numpy() for x in ax.BoundingVolumeHierarchy(v).export_nodes()]
+        assert all(np.array_equal(a, b) for a, b in zip(ref, got))
+    lo = uniform_points(3000, 78)
+    b = np.concatenate([lo, lo + 0.01], axis=1)
+    refb = [x.cpu().numpy() for x in ax.BoundingVolumeHierarchy(cuda(b), kind=1).export_nodes()]
+    bsoa = cuda(np.ascontiguousarray(b.T)).t()
+    gotb = [x.cpu().numpy() for x in ax.BoundingVolumeHierarchy(bsoa, kind=1).export_nodes()]
+    assert all(np.array_equal(x, y) for x, y in zip(refb, gotb))
