@@ -58,6 +58,15 @@ abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const floa
 abx_status single_leaf(cudaStream_t s, abx_geometry kind, const float *d_g,
                        LeafNode *d_leaves, TNode *d_tnodes, float4 *d_sorted, float *d_bounds);
 
+// Spatial queries with the default (two-pass) policy: from this many queries
+// on, a buffer of about twice the sampled mean hit count takes the counting
+// pass's results (up to kOnePassMaxBuffer per query and kOnePassMaxBytes in
+// all), and only overflowing queries are traversed again.
+constexpr int64_t kOnePassMinQueries = 65536;
+constexpr int64_t kOnePassSample = 4096;
+constexpr int64_t kOnePassMaxBuffer = 256;
+constexpr int64_t kOnePassMaxBytes = (int64_t)4 << 30;
+
 // Leaves per CTA of the block-local hierarchy climb.
 constexpr int kHierBlock = 256;
 
@@ -116,6 +125,19 @@ abx_status launch_spatial(cudaStream_t s, TreeView const &t, ForestView const *f
 
 abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int32_t buffer,
                           const int32_t *d_offsets, int32_t *d_out);
+
+// The queries whose result count (from CRS offsets) exceeds `buffer`, into
+// d_list (nq entries of room); their number in *h_count (synchronises s).
+abx_status launch_overflow_list(cudaStream_t s, const int32_t *d_offsets, int64_t nq,
+                                int32_t buffer, uint32_t *d_list, int64_t *h_count);
+
+// Mean number of results per query over a strided sample of at most
+// max_sample queries (counts land in d_counts at the sampled queries;
+// synchronises s).
+abx_status sample_mean_hits(cudaStream_t s, TreeView const &t, ForestView const *f,
+                            abx_geometry pred_kind, const float *d_preds, int64_t nq,
+                            const uint32_t *d_perm, int32_t *d_counts, int64_t max_sample,
+                            double *h_mean);
 
 // kNN: d_offsets null means uniform k (offset q * min(k, n)), and then
 // d_offsets_out (nq + 1) is filled by the kernel.  max_k bounds every k.

@@ -2,6 +2,7 @@
 // tree construction pipeline, CRS query drivers, result objects, per-device
 // state and error reporting.
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdlib>
 #include <cstring>
@@ -405,8 +406,22 @@ abx_status query_intersects(const abx_bvh *bvh, cudaStream_t s, abx_geometry kin
       return bail(st);
   }
   const TreeView tv = view_of(bvh);
-  const int64_t buffer = policy.buffer_size < 0 ? -(int64_t)policy.buffer_size
-                                                : (int64_t)policy.buffer_size;
+  int64_t buffer = policy.buffer_size < 0 ? -(int64_t)policy.buffer_size
+                                          : (int64_t)policy.buffer_size;
+  if (buffer == 0 && nq >= kOnePassMinQueries && tuning_value("SPATIAL_ONE_PASS", 1))
+  {
+    // same CRS result in about one traversal: a buffer sized from a sample
+    // of the queries takes the results of the counting pass; only the
+    // queries that overflow it are traversed again
+    double mean = 0;
+    abx_status st = sample_mean_hits(s, tv, f, kind, d_predicates, nq, perm.ptr, c->offsets,
+                                     kOnePassSample, &mean);
+    if (st != ABX_SUCCESS)
+      return bail(st);
+    const int64_t b = ((int64_t)std::ceil(2.0 * mean + 8.0) + 7) / 8 * 8;
+    if (b <= kOnePassMaxBuffer && b * nq * (int64_t)sizeof(int32_t) <= kOnePassMaxBytes)
+      buffer = b;
+  }
   int32_t total = 0;
   if (buffer == 0)
   {
@@ -454,11 +469,19 @@ abx_status query_intersects(const abx_bvh *bvh, cudaStream_t s, abx_geometry kin
                            " is too small for the results of some query"));
     if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
       return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
-    if (!overflow)
-      st = launch_compact(s, tmp.ptr, nq, (int32_t)buffer, c->offsets, c->indices);
-    else
-      st = launch_spatial(s, tv, f, kind, d_predicates, nq, perm.ptr, kFill, nullptr, c->offsets,
-                          c->indices, 0, nullptr);
+    st = launch_compact(s, tmp.ptr, nq, (int32_t)buffer, c->offsets, c->indices);
+    if (st == ABX_SUCCESS && overflow)
+    {
+      // traverse again only the queries whose results did not fit
+      Scratch<uint32_t> list;
+      int64_t m = 0;
+      if (list.alloc(nq, s) != cudaSuccess)
+        return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "overflow list"));
+      st = launch_overflow_list(s, c->offsets, nq, (int32_t)buffer, list.ptr, &m);
+      if (st == ABX_SUCCESS && m > 0)
+        st = launch_spatial(s, tv, f, kind, d_predicates, m, list.ptr, kFill, nullptr, c->offsets,
+                            c->indices, 0, nullptr);
+    }
     if (st != ABX_SUCCESS)
       return bail(st);
   }

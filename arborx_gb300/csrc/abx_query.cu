@@ -321,10 +321,53 @@ __global__ void k_compact(const int32_t *__restrict__ tmp, int64_t nq, int32_t b
   if (q >= nq)
     return;
   const int32_t o = offsets[q];
-  const int32_t c = offsets[q + 1] - o;
+  // an overflowed query keeps its first `buffer` results here; the fill
+  // pass rewrites all of them
+  const int32_t c = min(offsets[q + 1] - o, buffer);
   const int32_t *src = tmp + q * (int64_t)buffer;
   for (int j = lane; j < c; j += 32)
     out[o + j] = src[j];
+}
+
+// Queries whose result count exceeds the buffer: flag[q] = 1.
+__global__ void k_overflow_flags(const int32_t *__restrict__ offsets, int64_t nq, int32_t buffer,
+                                 int32_t *__restrict__ flags)
+{
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq)
+    flags[q] = offsets[q + 1] - offsets[q] > buffer;
+}
+
+// list[pos[q]] = q for every flagged query (pos: exclusive scan of flags).
+__global__ void k_overflow_list(const int32_t *__restrict__ flags, const int32_t *__restrict__ pos,
+                                int64_t nq, uint32_t *__restrict__ list)
+{
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nq && flags[q])
+    list[pos[q]] = (uint32_t)q;
+}
+
+// Strided sample of the queries (in traversal order): sample[t] = query of
+// position t * stride.
+__global__ void k_sample_queries(const uint32_t *__restrict__ perm, int64_t stride, int64_t m,
+                                 uint32_t *__restrict__ sample)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < m)
+    sample[t] = perm ? perm[t * stride] : (uint32_t)(t * stride);
+}
+
+// Sum of counts[sample[t]] into *total (zeroed).
+__global__ void k_sample_sum(const int32_t *__restrict__ counts, const uint32_t *__restrict__ sample,
+                             int64_t m, unsigned long long *__restrict__ total)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long v = t < m ? (unsigned long long)counts[sample[t]] : 0ull;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0 && v)
+    atomicAdd(total, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -787,12 +830,15 @@ __device__ __forceinline__ int load_tile(float4 *tile, const float4 *__restrict_
 template <int PRED, int MODE, int KIND>
 __global__ void __launch_bounds__(kQueryThreads)
     k_brute_spatial(const float4 *__restrict__ values, int64_t n, const float *__restrict__ preds,
-                    int64_t nq, int32_t *__restrict__ counts, const int32_t *__restrict__ offsets,
-                    int32_t *__restrict__ out, int32_t buffer, unsigned *__restrict__ overflow)
+                    int64_t nq, const uint32_t *__restrict__ list, int32_t *__restrict__ counts,
+                    const int32_t *__restrict__ offsets, int32_t *__restrict__ out,
+                    int32_t buffer, unsigned *__restrict__ overflow)
 {
   __shared__ float4 tile[kBruteTile * (KIND == 1 ? 2 : 1)];
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool active = q < nq;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = t < nq;
+  // the predicate of thread t: list[t] when a query list is given
+  const int64_t q = active && list ? (int64_t)__ldg(list + t) : t;
   const auto pred = PredOf<PRED>::load(preds, active ? q : 0);
   int32_t *dst = nullptr;
   if (MODE == kFill && active)
@@ -991,7 +1037,7 @@ abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, ForestView const 
                                                             err)
 #define ABX_BRUTE(M)                                                                         \
   k_brute_spatial<PRED, M, KIND><<<blocks, kQueryThreads, 0, s>>>(                               \
-      t.sorted, t.n, d_preds, nq, d_counts, d_offsets, d_out, buffer, d_overflow)
+      t.sorted, t.n, d_preds, nq, d_perm, d_counts, d_offsets, d_out, buffer, d_overflow)
   if (!t.tnodes) // brute force: every predicate against every value
   {
     if (mode == kCount)
@@ -1114,6 +1160,57 @@ abx_status brute_pack(cudaStream_t s, abx_geometry kind, const float *d_g, int64
   else
     k_brute_pack<0><<<blocks, 256, 0, s>>>(d_g, n, d_values);
   ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
+
+abx_status launch_overflow_list(cudaStream_t s, const int32_t *d_offsets, int64_t nq,
+                                int32_t buffer, uint32_t *d_list, int64_t *h_count)
+{
+  *h_count = 0;
+  if (nq <= 0)
+    return ABX_SUCCESS;
+  Scratch<int32_t> flags, pos;
+  ABX_CUDA_TRY(flags.alloc(nq, s));
+  ABX_CUDA_TRY(pos.alloc(nq + 1, s));
+  const unsigned blocks = (unsigned)((nq + 255) / 256);
+  k_overflow_flags<<<blocks, 256, 0, s>>>(d_offsets, nq, buffer, flags.ptr);
+  ABX_CUDA_TRY(cudaGetLastError());
+  ABX_TRY(exclusive_scan_i32(s, flags.ptr, nq, pos.ptr));
+  k_overflow_list<<<blocks, 256, 0, s>>>(flags.ptr, pos.ptr, nq, d_list);
+  ABX_CUDA_TRY(cudaGetLastError());
+  int32_t count = 0;
+  ABX_CUDA_TRY(cudaMemcpyAsync(&count, pos.ptr + nq, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  ABX_CUDA_TRY(cudaStreamSynchronize(s));
+  *h_count = count;
+  return ABX_SUCCESS;
+}
+
+abx_status sample_mean_hits(cudaStream_t s, TreeView const &t, ForestView const *f,
+                            abx_geometry pred_kind, const float *d_preds, int64_t nq,
+                            const uint32_t *d_perm, int32_t *d_counts, int64_t max_sample,
+                            double *h_mean)
+{
+  *h_mean = 0;
+  if (nq <= 0)
+    return ABX_SUCCESS;
+  const int64_t m = std::min(nq, max_sample);
+  const int64_t stride = nq / m;
+  Scratch<uint32_t> sample;
+  Scratch<unsigned long long> total;
+  ABX_CUDA_TRY(sample.alloc(m, s));
+  ABX_CUDA_TRY(total.alloc(1, s));
+  ABX_CUDA_TRY(cudaMemsetAsync(total.ptr, 0, sizeof(unsigned long long), s));
+  const unsigned blocks = (unsigned)((m + 255) / 256);
+  k_sample_queries<<<blocks, 256, 0, s>>>(d_perm, stride, m, sample.ptr);
+  ABX_CUDA_TRY(cudaGetLastError());
+  ABX_TRY(launch_spatial(s, t, f, pred_kind, d_preds, m, sample.ptr, kCount, d_counts, nullptr,
+                         nullptr, 0, nullptr));
+  k_sample_sum<<<blocks, 256, 0, s>>>(d_counts, sample.ptr, m, total.ptr);
+  ABX_CUDA_TRY(cudaGetLastError());
+  unsigned long long sum = 0;
+  ABX_CUDA_TRY(cudaMemcpyAsync(&sum, total.ptr, sizeof(sum), cudaMemcpyDeviceToHost, s));
+  ABX_CUDA_TRY(cudaStreamSynchronize(s));
+  *h_mean = (double)sum / (double)m;
   return ABX_SUCCESS;
 }
 

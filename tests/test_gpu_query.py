@@ -285,3 +285,31 @@ def _check_variant_results(ax, bvh, ref, q):
     assert np.array_equal(host(off), roff) and np.array_equal(host(ind), rind)
     assert ax.device_errors() == 0
 
+
+
+def test_one_pass_spatial_equals_two_pass(ax):
+    # default policy: from 65536 queries on, a sampled buffer takes the
+    # counting pass's results and only overflowing queries are traversed
+    # again; the CRS (order included) equals the plain two-pass result
+    L = ax._lib.load()
+    p = uniform_points(300000, 141)
+    q = uniform_points(150000, 142)
+    rng = np.random.default_rng(7)
+    r = np.where(rng.random(q.shape[0]) < 0.02, 0.08, 0.012).astype(np.float32)  # 2% heavy
+    spheres = np.concatenate([q, r[:, None]], axis=1)
+    bvh = ax.BoundingVolumeHierarchy(cuda(p))
+    ref = o.OracleTree(p)
+    roff, rind = ref.spatial(o.KIND_SPHERE, spheres)
+    try:
+        for one_pass in (0, 1):
+            ax._lib.check(L.abx_tuning_set(b"SPATIAL_ONE_PASS", one_pass))
+            for sort in (True, False):
+                pol = ax.TraversalPolicy().setPredicateSorting(sort)
+                ind, off = ax.query(bvh, ax.intersects(cuda(spheres)), pol)
+                assert np.array_equal(host(off), roff) and np.array_equal(host(ind), rind)
+        # an explicit small buffer overflows for the heavy queries only
+        ind, off = ax.query(bvh, ax.intersects(cuda(spheres)), ax.TraversalPolicy().setBufferSize(8))
+        assert np.array_equal(host(off), roff) and np.array_equal(host(ind), rind)
+    finally:
+        L.abx_tuning_reset()
+    assert ax.device_errors() == 0
