@@ -23,6 +23,9 @@ from .bvh import (  # noqa: F401
     TraversalPolicy,
     device_errors,
     exclusive_scan,
+    expand_half_to_full,
+    find_full_neighbor_list,
+    find_half_neighbor_list,
     generate_hierarchy,
     intersects,
     make_intersects,

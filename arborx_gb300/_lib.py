@@ -126,6 +126,8 @@ SIGNATURES = {
     "abx_bvh_query_nearest_into": (
         _STATUS, [_P, _P, _P, _I64, _I32, TraversalPolicyC, _P, _P, _P],
     ),
+    "abx_find_neighbor_list": (_STATUS, [_P, _P, _I64, ctypes.c_float, _I32, ctypes.POINTER(_P)]),
+    "abx_expand_half_to_full": (_STATUS, [_P, _I64, _P, _P, ctypes.POINTER(_P)]),
     "abx_crs_num_queries": (_I64, [_P]),
     "abx_crs_num_results": (_I64, [_P]),
     "abx_crs_offsets": (_P, [_P]),

@@ -308,6 +308,42 @@ def query_nearest_into(tree, queries, k, offsets, indices, distances=None, polic
         _ptr(indices), _ptr(distances) if distances is not None else None))
 
 
+def _neighbor_list(points, radius, half, space):
+    p = _as_rows(points, 3, "points")
+    h = ctypes.c_void_p()
+    check(_lib.load().abx_find_neighbor_list(_stream(space), _ptr(p), p.shape[0], float(radius),
+                                             1 if half else 0, ctypes.byref(h)))
+    indices, offsets = _crs_result(h, False)
+    return offsets, indices
+
+
+def find_full_neighbor_list(points, radius, space=None):
+    """ArborX::Experimental::findFullNeighborList (ArborX_NeighborList.hpp:
+    113-186): (offsets, indices), row p = every other point within radius,
+    in the tree's depth-first order."""
+    return _neighbor_list(points, radius, False, space)
+
+
+def find_half_neighbor_list(points, radius, space=None):
+    """ArborX::Experimental::findHalfNeighborList (ArborX_NeighborList.hpp:
+    47-111): (offsets, indices), row p = the points within radius whose leaf
+    precedes p's in the tree's Morton order (each pair once)."""
+    return _neighbor_list(points, radius, True, space)
+
+
+def expand_half_to_full(offsets, indices, space=None):
+    """ArborX::Details::expandHalfToFull (ArborX_ExpandHalfToFull.hpp:23-69):
+    (offsets, indices) of the full list; row i = its half row, then the rows
+    listing i in ascending order."""
+    h = ctypes.c_void_p()
+    o = offsets.to(torch.int32).contiguous()
+    i = indices.to(torch.int32).contiguous()
+    check(_lib.load().abx_expand_half_to_full(_stream(space), o.numel() - 1, _ptr(o), _ptr(i),
+                                              ctypes.byref(h)))
+    ind, off = _crs_result(h, False)
+    return off, ind
+
+
 def _crs_result(h, with_distances):
     L = _lib.load()
     owner = _CrsOwner(h)

@@ -126,6 +126,26 @@ abx_status launch_spatial(cudaStream_t s, TreeView const &t, ForestView const *f
 abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int32_t buffer,
                           const int32_t *d_offsets, int32_t *d_out);
 
+// Spatial self-query of a point tree with spheres built from its own values
+// (neighbor lists): filter 1 drops each value from its own result, filter 2
+// keeps only values whose leaf precedes the query value's leaf
+// (d_leaf_pos[value] = Morton position).  Count and fill modes.
+abx_status launch_spatial_self(cudaStream_t s, TreeView const &t, int filter,
+                               const int32_t *d_leaf_pos, const float *d_spheres, int64_t nq,
+                               const uint32_t *d_perm, SpatialMode mode, int32_t *d_counts,
+                               const int32_t *d_offsets, int32_t *d_out);
+
+// Neighbor lists: spheres (p, r) of every point; the tree's leaf order
+// (order[t] = value at Morton position t, pos[value] = t); the full list from
+// a half list (row i = its half row, then the rows k listing i, ascending k).
+abx_status self_spheres(cudaStream_t s, const float *d_points, int64_t n, float r,
+                        float *d_spheres);
+abx_status leaf_order(cudaStream_t s, const float4 *d_sorted, int64_t n, uint32_t *d_order,
+                      int32_t *d_pos);
+abx_status expand_half_to_full(cudaStream_t s, int64_t n, const int32_t *d_half_off,
+                               const int32_t *d_half_idx, int64_t m, int32_t *d_full_off,
+                               int32_t *d_full_idx);
+
 // The queries whose result count (from CRS offsets) exceeds `buffer`, into
 // d_list (nq entries of room); their number in *h_count (synchronises s).
 abx_status launch_overflow_list(cudaStream_t s, const int32_t *d_offsets, int64_t nq,

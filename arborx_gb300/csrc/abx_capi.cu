@@ -7,6 +7,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <new>
 #include <string>
@@ -1128,6 +1129,112 @@ abx_status abx_brute_query_nearest(const abx_brute *brute, void *stream, const f
                                    abx_crs **out)
 {
   return abx_bvh_query_nearest(brute, stream, d_queries, nq, d_k, k, policy, with_distances, out);
+}
+
+abx_status abx_find_neighbor_list(void *stream, const float *d_points, int64_t n, float radius,
+                                  int32_t half, abx_crs **out)
+{
+  if (!out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_find_neighbor_list: null output");
+  *out = nullptr;
+  if (n < 0 || n >= (int64_t)INT32_MAX || (n > 0 && !d_points))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_find_neighbor_list: bad points");
+  cudaStream_t s = as_stream(stream);
+  abx_bvh *t = nullptr;
+  ABX_TRY(abx_bvh_create(stream, ABX_POINT, d_points, n, &t));
+  std::unique_ptr<abx_bvh, void (*)(abx_bvh *)> tree(t, destroy_tree);
+  abx_crs *c = new (std::nothrow) abx_crs;
+  if (!c)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
+  cudaGetDevice(&c->device);
+  c->stream = s;
+  c->nq = n;
+  auto bail = [&](abx_status st) {
+    cudaStreamSynchronize(s);
+    destroy_crs(c);
+    return st;
+  };
+  if (dmalloc_n(&c->offsets, n + 1, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS offsets"));
+  if (n <= 1)
+  {
+    cudaMemsetAsync(c->offsets, 0, (n + 1) * sizeof(int32_t), s);
+    dmalloc_n(&c->indices, 0, s);
+    *out = c;
+    return ABX_SUCCESS;
+  }
+  Scratch<float> spheres;
+  Scratch<uint32_t> order;
+  Scratch<int32_t> pos;
+  if (spheres.alloc(4 * n, s) != cudaSuccess || order.alloc(n, s) != cudaSuccess ||
+      pos.alloc(n, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "neighbor list scratch"));
+  // queries in the tree's leaf order: Morton-coherent without a sort
+  abx_status st = self_spheres(s, d_points, n, radius, spheres.ptr);
+  if (st == ABX_SUCCESS)
+    st = leaf_order(s, t->sorted, n, order.ptr, pos.ptr);
+  const TreeView tv = view_of(t);
+  const int filter = half ? 2 : 1;
+  if (st == ABX_SUCCESS)
+    st = launch_spatial_self(s, tv, filter, pos.ptr, spheres.ptr, n, order.ptr, kCount,
+                             c->offsets, nullptr, nullptr);
+  if (st == ABX_SUCCESS)
+    st = exclusive_scan_i32(s, c->offsets, n, c->offsets);
+  if (st != ABX_SUCCESS)
+    return bail(st);
+  int32_t total = 0;
+  cudaMemcpyAsync(&total, c->offsets + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s);
+  st = sync_and_check(s);
+  if (st != ABX_SUCCESS)
+    return bail(st);
+  if (dmalloc_n(&c->indices, (size_t)total, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS indices"));
+  st = launch_spatial_self(s, tv, filter, pos.ptr, spheres.ptr, n, order.ptr, kFill, nullptr,
+                           c->offsets, c->indices);
+  if (st != ABX_SUCCESS)
+    return bail(st);
+  c->nres = total;
+  *out = c;
+  return ABX_SUCCESS;
+}
+
+abx_status abx_expand_half_to_full(void *stream, int64_t n, const int32_t *d_offsets,
+                                   const int32_t *d_indices, abx_crs **out)
+{
+  if (!out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_expand_half_to_full: null output");
+  *out = nullptr;
+  if (n < 0 || n >= (int64_t)INT32_MAX || !d_offsets)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_expand_half_to_full: bad arguments");
+  cudaStream_t s = as_stream(stream);
+  device_state();
+  int32_t m = 0;
+  ABX_CUDA_TRY(cudaMemcpyAsync(&m, d_offsets + n, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  ABX_CUDA_TRY(cudaStreamSynchronize(s));
+  if (m < 0 || (int64_t)m * 2 >= (int64_t)INT32_MAX || (m > 0 && !d_indices))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_expand_half_to_full: bad half list");
+  abx_crs *c = new (std::nothrow) abx_crs;
+  if (!c)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
+  cudaGetDevice(&c->device);
+  c->stream = s;
+  c->nq = n;
+  auto bail = [&](abx_status st) {
+    cudaStreamSynchronize(s);
+    destroy_crs(c);
+    return st;
+  };
+  if (dmalloc_n(&c->offsets, n + 1, s) != cudaSuccess ||
+      dmalloc_n(&c->indices, (size_t)m * 2, s) != cudaSuccess)
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS"));
+  if (n == 0)
+    cudaMemsetAsync(c->offsets, 0, sizeof(int32_t), s);
+  abx_status st = expand_half_to_full(s, n, d_offsets, d_indices, m, c->offsets, c->indices);
+  if (st != ABX_SUCCESS)
+    return bail(st);
+  c->nres = 2 * (int64_t)m;
+  *out = c;
+  return ABX_SUCCESS;
 }
 
 int64_t abx_crs_num_queries(const abx_crs *crs) { return crs ? crs->nq : 0; }

@@ -185,13 +185,26 @@ __device__ __forceinline__ ChildKind child_kind(int ref, int cf, int bucket, int
   return kDescend;
 }
 
-template <int PRED, int MODE, int KIND>
+// Leaf filters of a self-query (predicate q built from the value q itself):
+// kKeepAll, kSkipSelf (a value never matches its own predicate) or
+// kEarlierLeaves (only values whose leaf precedes q's leaf in Morton order,
+// leaf_pos[value] = its position: the pairs of the reference's
+// HalfTraversal, ArborX_HalfTraversal.hpp:52-73).
+enum LeafFilter
+{
+  kKeepAll = 0,
+  kSkipSelf = 1,
+  kEarlierLeaves = 2
+};
+
+template <int PRED, int MODE, int KIND, int FILTER = kKeepAll>
 __global__ void __launch_bounds__(kQueryThreads)
     k_spatial(const TNode *__restrict__ nodes, const float4 *__restrict__ sorted, int64_t n,
               ForestView f, const float *__restrict__ preds, int64_t nq,
               const uint32_t *__restrict__ perm, int32_t *__restrict__ counts,
               const int32_t *__restrict__ offsets, int32_t *__restrict__ out, int32_t buffer,
-              int bucket, unsigned *__restrict__ overflow, unsigned *__restrict__ err)
+              int bucket, unsigned *__restrict__ overflow, unsigned *__restrict__ err,
+              const int32_t *__restrict__ leaf_pos = nullptr)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nq)
@@ -216,7 +229,12 @@ __global__ void __launch_bounds__(kQueryThreads)
     cap = buffer;
   }
   int32_t count = 0;
+  const int32_t own_pos = FILTER == kEarlierLeaves ? __ldg(leaf_pos + q) : 0;
   auto emit = [&](int v) {
+    if (FILTER == kSkipSelf && v == q)
+      return;
+    if (FILTER == kEarlierLeaves && __ldg(leaf_pos + v) >= own_pos)
+      return;
     if (MODE == kFill)
       dst[count] = v;
     if (MODE == kBuffered && count < cap)
@@ -1159,6 +1177,44 @@ abx_status brute_pack(cudaStream_t s, abx_geometry kind, const float *d_g, int64
     k_brute_pack<1><<<blocks, 256, 0, s>>>(d_g, n, d_values);
   else
     k_brute_pack<0><<<blocks, 256, 0, s>>>(d_g, n, d_values);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
+
+abx_status launch_spatial_self(cudaStream_t s, TreeView const &t, int filter,
+                               const int32_t *d_leaf_pos, const float *d_spheres, int64_t nq,
+                               const uint32_t *d_perm, SpatialMode mode, int32_t *d_counts,
+                               const int32_t *d_offsets, int32_t *d_out)
+{
+  if (nq <= 0 || t.n <= 0)
+    return ABX_SUCCESS;
+  if (t.kind != ABX_POINT || !t.tnodes)
+    return fail(ABX_ERROR_NOT_SUPPORTED, "neighbor lists: point trees only");
+  unsigned *err = device_state().d_error;
+  const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
+  const int bucket =
+      std::max(1, std::min(kMaxBucket, tuning_value("SPATIAL_BUCKET", kDefaultSpatialBucket)));
+  const ForestView f{nullptr, nullptr, 1};
+  StageScope scope(s, "spatial", 1);
+#define ABX_SELF(M, F)                                                                          \
+  k_spatial<ABX_SPHERE, M, 0, F><<<blocks, kQueryThreads, 0, s>>>(                              \
+      t.tnodes, t.sorted, t.n, f, d_spheres, nq, d_perm, d_counts, d_offsets, d_out, 0, bucket, \
+      nullptr, err, d_leaf_pos)
+  if (filter == kSkipSelf)
+  {
+    if (mode == kCount)
+      ABX_SELF(kCount, kSkipSelf);
+    else
+      ABX_SELF(kFill, kSkipSelf);
+  }
+  else
+  {
+    if (mode == kCount)
+      ABX_SELF(kCount, kEarlierLeaves);
+    else
+      ABX_SELF(kFill, kEarlierLeaves);
+  }
+#undef ABX_SELF
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
 }

@@ -281,6 +281,27 @@ ABX_API abx_status abx_forest_query_nearest(const abx_forest *forest,
                                             abx_crs **out);
 
 /* ---------------------------------------------------------------------- */
+/* Neighbor lists (src/spatial/detail/ArborX_NeighborList.hpp:47-188)      */
+/* ---------------------------------------------------------------------- */
+/* findFullNeighborList / findHalfNeighborList(space, points, radius,
+ * offsets, indices): the radius self-join of n points (a tree is built
+ * internally).  Full (half = 0): row p lists every other point q with
+ * distance(p, q) <= radius.  Half (half != 0): row p lists the points q
+ * within radius whose leaf precedes p's leaf in the tree's Morton order (the
+ * pairs of HalfTraversal, ArborX_HalfTraversal.hpp:52-73), so every pair
+ * appears once.  The reference fills rows through atomics (any order); here a
+ * row is in the tree's depth-first order.  CRS over n rows. */
+ABX_API abx_status abx_find_neighbor_list(void *stream, const float *d_points, int64_t n,
+                                          float radius, int32_t half, abx_crs **out);
+
+/* expandHalfToFull (src/spatial/detail/ArborX_ExpandHalfToFull.hpp:23-69):
+ * from a half list (device offsets n + 1, indices) the full list, row i = its
+ * half row followed by every k whose half row lists i, in ascending k.
+ * Synchronises once (the input size). */
+ABX_API abx_status abx_expand_half_to_full(void *stream, int64_t n, const int32_t *d_offsets,
+                                           const int32_t *d_indices, abx_crs **out);
+
+/* ---------------------------------------------------------------------- */
 /* Brute force (src/spatial/ArborX_BruteForce.hpp:40-176)                  */
 /* ---------------------------------------------------------------------- */
 /* BruteForce(space, values): every predicate is tested against every value

@@ -139,6 +139,29 @@ def crs_query_impl():
     return {"n": n, "buffer_size": 2 * (n + 1), "offsets": offsets, "indices": indices}
 
 
+def neighbor_lists(root):
+    """test/tstNeighborList.cpp:109-171: full neighbor lists (offsets,
+    indices) of four points on the diagonal for several radii, and the
+    degenerate empty / single-point clouds with an infinite radius.  The
+    reference compares rows as multisets."""
+    src = _read(root, "test/tstNeighborList.cpp")
+    body = src[src.index("BOOST_AUTO_TEST_CASE_TEMPLATE(find_neighbor_list,"):]
+    pts_txt = body[body.index("std::vector<Point>{") + len("std::vector<Point>{"):body.index('"Test::four_points"')]
+    points = [[float(v.rstrip("f")) for v in t.split(",")]
+              for t in re.findall(r"\{([-0-9.f, ]+)\}", pts_txt)]
+    cases = []
+    pat = re.compile(r"ARBORX_TEST_NEIGHBOR_LIST\(\s*exec_space,\s*points,\s*\(Coordinate\)([0-9.]+),\s*"
+                     r"\(std::vector<int>\{([0-9, ]*)\}\),\s*\(std::vector<int>\{([0-9, ]*)\}\)\)", re.S)
+    for r, off, idx in pat.findall(body):
+        cases.append({"radius": float(r),
+                      "offsets": [int(x) for x in off.replace(" ", "").split(",") if x],
+                      "indices": [int(x) for x in idx.replace(" ", "").split(",") if x]})
+    assert len(points) == 4 and len(cases) == 4, (points, cases)
+    return {"cite": "test/tstNeighborList.cpp:109-171", "points": points, "cases": cases,
+            "degenerate": [{"n": 0, "offsets": [0], "indices": []},
+                           {"n": 1, "offsets": [0, 0], "indices": []}]}
+
+
 def main(root):
     data = {
         "source": "ArborX 2.1.99 test sources (read as text)",
@@ -147,6 +170,7 @@ def main(root):
         "assign_morton_codes": assign_morton_codes(root),
         "degenerate": degenerate_cases(),
         "crs_query_impl": crs_query_impl(),
+        "neighbor_lists": neighbor_lists(root),
         "stack_capacity": {"cite": "tstQueryTreeDegenerate.cpp:367-446", "n": 4096},
         "manufactured_grid": {"cite": "tstQueryTreeManufacturedSolution.cpp:64-269", "nx": 11, "L": 100.0},
     }

@@ -189,3 +189,16 @@ def test_oracle_duplicates_and_line():
         bi, bd = o.knn_brute(p, q, 7)
         assert np.array_equal(ind.reshape(-1, 7), bi)
         assert np.array_equal(dist.reshape(-1, 7), bd)
+
+
+def test_oracle_neighbor_lists_golden(golden):
+    """test/tstNeighborList.cpp:136-171: full neighbor lists of four points on
+    the diagonal (rows compared as multisets, as the reference does)."""
+    nl = golden["neighbor_lists"]
+    pts = np.asarray(nl["points"], np.float32)
+    for case in nl["cases"]:
+        sph = np.concatenate([pts, np.full((4, 1), case["radius"], np.float32)], axis=1)
+        off, ind = o.spatial_brute(pts, o.KIND_SPHERE, sph)
+        rows = [sorted(int(v) for v in ind[off[i]:off[i + 1]] if v != i) for i in range(4)]
+        want = [sorted(case["indices"][case["offsets"][i]:case["offsets"][i + 1]]) for i in range(4)]
+        assert rows == want
