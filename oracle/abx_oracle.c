@@ -1178,3 +1178,152 @@ void abxo_visit_counts(int64_t n, int is_box, const float *geom,
   *out_internal = vi;
   *out_leaves = vl;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Rays                                                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Ray{origin, direction} (src/geometry/ArborX_Ray.hpp:33-66): the constructor
+ * normalizes the direction in double (misc/ArborX_Vector.hpp:40-88): the
+ * double norm sqrt(((0 + x*x) + y*y) + z*z) of the float components, each
+ * component divided by it in double and rounded to float.  Rows of 6 floats. */
+void abxo_ray_normalize(const float *raw, int64_t n, float *out)
+{
+  for (int64_t i = 0; i < n; ++i)
+  {
+    const float *r = raw + 6 * i;
+    double s = 0;
+    for (int d = 0; d < 3; ++d)
+      s += (double)r[3 + d] * (double)r[3 + d];
+    const double mag = sqrt(s);
+    for (int d = 0; d < 3; ++d)
+    {
+      out[6 * i + d] = r[d];
+      out[6 * i + 3 + d] = (float)((double)r[3 + d] / mag);
+    }
+  }
+}
+
+/* intersection(Ray, Box, tmin, tmax) (ArborX_Ray.hpp:107-158): the slab test
+ * with a zero direction component handled through the signs, and the
+ * comparisons written so that a NaN never updates tmin / tmax. */
+int abxo_ray_box_intersection(const float *ray, const float *box, float *tmin_out,
+                              float *tmax_out)
+{
+  const float inf = INFINITY;
+  float tmin = -inf, tmax = inf;
+  for (int d = 0; d < 3; ++d)
+  {
+    const float o = ray[d], dir = ray[3 + d], lo = box[d], hi = box[3 + d];
+    float tdmin, tdmax;
+    if (dir == 0)
+    {
+      const float min_orig = lo - o;
+      if (min_orig == 0)
+        continue;
+      const float max_orig = hi - o;
+      tdmin = signbit(dir * max_orig) ? inf : -inf;
+      tdmax = signbit(dir * min_orig) ? inf : -inf;
+    }
+    else if (dir > 0)
+    {
+      tdmin = (lo - o) / dir;
+      tdmax = (hi - o) / dir;
+    }
+    else
+    {
+      tdmin = (hi - o) / dir;
+      tdmax = (lo - o) / dir;
+    }
+    if (tmin < tdmin)
+      tmin = tdmin;
+    if (tmax > tdmax)
+      tmax = tdmax;
+  }
+  *tmin_out = tmin;
+  *tmax_out = tmax;
+  return tmin <= tmax;
+}
+
+/* intersects(Ray, Box) (ArborX_Ray.hpp:160-168) and distance(Ray, Box)
+ * (:435-447): the entry distance max(tmin, 0) of a box in front of the ray,
+ * +inf otherwise. */
+int abxo_ray_box_intersects(const float *ray, const float *box)
+{
+  float t0, t1;
+  return abxo_ray_box_intersection(ray, box, &t0, &t1) && t1 >= 0;
+}
+
+float abxo_ray_box_distance(const float *ray, const float *box)
+{
+  float t0, t1;
+  const int hit = abxo_ray_box_intersection(ray, box, &t0, &t1) && t1 >= 0;
+  return hit ? (t0 < 0.f ? 0.f : t0) : INFINITY;
+}
+
+/* Brute force over n values (points as degenerate boxes) for nq normalized
+ * rays: intersects (ordered = 0: ascending index) or ordered_intersects
+ * (ordered = 1: ascending (distance, index)).  Two calls: indices NULL
+ * returns the total and fills offsets. */
+int64_t abxo_ray_brute(const float *geom, int64_t n, int is_box, const float *rays, int64_t nq,
+                       int ordered, int32_t *offsets, int32_t *indices, float *dist)
+{
+  int64_t total = 0;
+  typedef struct
+  {
+    float d;
+    int32_t i;
+  } hit_t;
+  hit_t *hits = indices ? (hit_t *)malloc(sizeof(hit_t) * (size_t)(n > 0 ? n : 1)) : NULL;
+  if (offsets)
+    offsets[0] = 0;
+  for (int64_t q = 0; q < nq; ++q)
+  {
+    const float *ray = rays + 6 * q;
+    int64_t m = 0;
+    for (int64_t j = 0; j < n; ++j)
+    {
+      float b[6];
+      for (int d = 0; d < 3; ++d)
+      {
+        b[d] = geom[(is_box ? 6 : 3) * j + d];
+        b[3 + d] = geom[(is_box ? 6 : 3) * j + (is_box ? 3 : 0) + d];
+      }
+      if (abxo_ray_box_intersects(ray, b))
+      {
+        if (hits)
+        {
+          hits[m].d = abxo_ray_box_distance(ray, b);
+          hits[m].i = (int32_t)j;
+        }
+        ++m;
+      }
+    }
+    if (hits)
+    {
+      if (ordered) /* insertion sort by (distance, index) */
+        for (int64_t a = 1; a < m; ++a)
+        {
+          hit_t h = hits[a];
+          int64_t b = a - 1;
+          while (b >= 0 && (hits[b].d > h.d || (hits[b].d == h.d && hits[b].i > h.i)))
+          {
+            hits[b + 1] = hits[b];
+            --b;
+          }
+          hits[b + 1] = h;
+        }
+      for (int64_t a = 0; a < m; ++a)
+      {
+        indices[total + a] = hits[a].i;
+        if (dist)
+          dist[total + a] = hits[a].d;
+      }
+    }
+    total += m;
+    if (offsets)
+      offsets[q + 1] = (int32_t)total;
+  }
+  free(hits);
+  return total;
+}

@@ -78,6 +78,15 @@ def lib():
         L.abxo_spatial_brute.argtypes = [P, I64, I, I, P, I64, P, P]
         L.abxo_exclusive_scan_i32.argtypes = [P, I64, P]
         L.abxo_visit_counts.argtypes = [I64, I, P, P, P, I, I, P, I64, I32, P, P]
+        L.abxo_ray_normalize.argtypes = [P, I64, P]
+        L.abxo_ray_box_intersection.restype = I
+        L.abxo_ray_box_intersection.argtypes = [P, P, P, P]
+        L.abxo_ray_box_intersects.restype = I
+        L.abxo_ray_box_intersects.argtypes = [P, P]
+        L.abxo_ray_box_distance.restype = ctypes.c_float
+        L.abxo_ray_box_distance.argtypes = [P, P]
+        L.abxo_ray_brute.restype = I64
+        L.abxo_ray_brute.argtypes = [P, I64, I, P, I64, I, P, P, P]
         L.abxo_num_threads.restype = I
         L.abxo_set_num_threads.argtypes = [I]
         _lib = L
@@ -93,6 +102,51 @@ def _f32(a, cols):
     if a.size == 0:
         return a.reshape(0, cols)
     return a.reshape(-1, cols)
+
+
+def ray_normalize(rays):
+    """Ray{origin, direction} construction (ArborX_Ray.hpp:46-55): rows of 6
+    floats with the direction normalized as the reference does."""
+    r = _f32(rays, 6)
+    out = np.empty_like(r)
+    lib().abxo_ray_normalize(_p(r), r.shape[0], _p(out))
+    return out
+
+
+def ray_box_intersection(ray, box):
+    """(hit, tmin, tmax) of intersection(Ray, Box) (ArborX_Ray.hpp:107-158);
+    ray already normalized."""
+    r = _f32(ray, 6)
+    b = _f32(box, 6)
+    t0 = np.zeros(1, np.float32)
+    t1 = np.zeros(1, np.float32)
+    hit = lib().abxo_ray_box_intersection(_p(r), _p(b), _p(t0), _p(t1))
+    return bool(hit), float(t0[0]), float(t1[0])
+
+
+def ray_box_intersects(ray, box):
+    return bool(lib().abxo_ray_box_intersects(_p(_f32(ray, 6)), _p(_f32(box, 6))))
+
+
+def ray_box_distance(ray, box):
+    return lib().abxo_ray_box_distance(_p(_f32(ray, 6)), _p(_f32(box, 6)))
+
+
+def ray_brute(geom, rays, ordered, is_box=True):
+    """CRS (offsets, indices, distances) of intersects(ray) (ascending index)
+    or ordered_intersects(ray) (ascending (distance, index)) by brute force;
+    rays already normalized."""
+    g = _f32(geom, 6 if is_box else 3)
+    r = _f32(rays, 6)
+    nq = r.shape[0]
+    offsets = np.zeros(nq + 1, np.int32)
+    total = lib().abxo_ray_brute(_p(g), g.shape[0], int(is_box), _p(r), nq, int(ordered),
+                                 _p(offsets), None, None)
+    indices = np.empty(total, np.int32)
+    dist = np.empty(total, np.float32)
+    lib().abxo_ray_brute(_p(g), g.shape[0], int(is_box), _p(r), nq, int(ordered), _p(offsets),
+                         _p(indices), _p(dist))
+    return offsets, indices, dist
 
 
 def num_threads():

@@ -162,6 +162,56 @@ def neighbor_lists(root):
                            {"n": 1, "offsets": [0, 0], "indices": []}]}
 
 
+def _f32_expr(txt):
+    """Value of a test's float expression like -.5f*sqrtf_2 or 2*sqrtf_3,
+    evaluated in float32 as the test does (sqrtf_k = std::sqrt(k.f))."""
+    import numpy as np
+
+    env = {"sqrtf_%d" % k: np.sqrt(np.float32(k)) for k in (2, 3, 5)}
+    t = txt.strip().replace("f", "") if "sqrtf" not in txt else txt.strip()
+    t = re.sub(r"(?<![a-z_])([0-9]*\.?[0-9]+)f", r"\1", t)
+    v = eval(t, {"np": np}, {k: v for k, v in env.items()})
+    return float(np.float32(v))
+
+
+def rays(root):
+    """test/tstRay.cpp:17-275 (intersects_box, ray_box_intersection with a
+    1e-6 tolerance, ray_box_distance) against the unit box, and
+    test/tstQueryTreeRay.cpp:62-265 (ten diagonal boxes; ordered results,
+    empty and one-leaf trees).  Rays as written in the test (the library
+    normalizes the direction)."""
+    src = _read(root, "test/tstRay.cpp")
+    num = r"[-0-9.]+"
+    ray = r"Ray\{\{(%s), (%s), (%s)\}, \{(%s), (%s), (%s)\}\}" % ((num,) * 6)
+    inter = [{"ray": [float(x) for x in m[1:]], "hit": m[0] == ""}
+             for m in re.findall(r"BOOST_TEST\((!?)intersects\(" + ray + r", unit_box\)\);", src)]
+    vals = []
+    for m in re.finditer(r"ARBORX_TEST_RAY_BOX_INTERSECTION\(\(" + ray + r"\), unit_box, ?([^,]+), ([^)]+)\);", src):
+        g = m.groups()
+        vals.append({"ray": [float(x) for x in g[:6]], "t0": _f32_expr(g[6]), "t1": _f32_expr(g[7])})
+    for m in re.finditer(r"ARBORX_TEST_RAY_BOX_NO_INTERSECTION\(\(" + ray + r"\), unit_box\);", src):
+        vals.append({"ray": [float(x) for x in m.groups()], "hit": False})
+    dist = []
+    for m in re.finditer(r"BOOST_TEST\(distance\(" + ray + r", unit_box\) == ([^)]+)\);", src):
+        g = m.groups()
+        d = g[6].strip()
+        dist.append({"ray": [float(x) for x in g[:6]], "distance": "inf" if d == "inf" else float(d.rstrip("f"))})
+    assert len(inter) >= 40 and len(vals) >= 40 and len(dist) == 3, (len(inter), len(vals), len(dist))
+    n = 10
+    boxes = [[i, i, i, i + 1, i + 1, i + 1] for i in range(n)]
+    return {"cite": "test/tstRay.cpp:17-275, test/tstQueryTreeRay.cpp:62-265",
+            "unit_box": [0, 0, 0, 1, 1, 1], "intersects_box": inter, "intersection": vals,
+            "distance": dist,
+            "tree_boxes": boxes,
+            "tree_intersects": {"ray": [0, 0, 0, .1, .1, .1], "indices": list(range(n))},
+            "tree_ordered": [{"ray": [0, 0, 0, 1 / n, 1 / n, 1 / n], "indices": list(range(n))},
+                             {"ray": [n, n, n, -1 / n, -1 / n, -1 / n], "indices": list(range(n - 1, -1, -1))}],
+            "tree_nearest": {"ray": [0, 0, 0, .15, .1, 0], "k": 1, "indices": [0]},
+            "single_leaf": {"box": [0, 0, 0, 1, 1, 1],
+                            "rays": [[0, 0, 0, 1, 1, 1], [4, 5, 6, 7, 8, 9]], "offsets": [0, 1, 1],
+                            "indices": [0]}}
+
+
 def main(root):
     data = {
         "source": "ArborX 2.1.99 test sources (read as text)",
@@ -171,6 +221,7 @@ def main(root):
         "degenerate": degenerate_cases(),
         "crs_query_impl": crs_query_impl(),
         "neighbor_lists": neighbor_lists(root),
+        "rays": rays(root),
         "stack_capacity": {"cite": "tstQueryTreeDegenerate.cpp:367-446", "n": 4096},
         "manufactured_grid": {"cite": "tstQueryTreeManufacturedSolution.cpp:64-269", "nx": 11, "L": 100.0},
     }

@@ -202,3 +202,43 @@ def test_oracle_neighbor_lists_golden(golden):
         rows = [sorted(int(v) for v in ind[off[i]:off[i + 1]] if v != i) for i in range(4)]
         want = [sorted(case["indices"][case["offsets"][i]:case["offsets"][i + 1]]) for i in range(4)]
         assert rows == want
+
+
+def test_oracle_rays_golden(golden):
+    """test/tstRay.cpp:17-275: ray-box intersects / intersection (tolerance
+    1e-6 as the test) / distance against the unit box, rays normalized as the
+    Ray constructor does."""
+    g = golden["rays"]
+    box = np.asarray(g["unit_box"], np.float32)
+    for c in g["intersects_box"]:
+        ray = o.ray_normalize(np.asarray(c["ray"], np.float32))[0]
+        assert o.ray_box_intersects(ray, box) == c["hit"], c
+    for c in g["intersection"]:
+        ray = o.ray_normalize(np.asarray(c["ray"], np.float32))[0]
+        hit, t0, t1 = o.ray_box_intersection(ray, box)
+        if "hit" in c and not c["hit"]:
+            assert not hit and (t0 == np.inf or t1 == -np.inf), c
+        else:
+            assert hit, c
+            assert t0 == pytest.approx(c["t0"], rel=1e-6, abs=1e-30), c
+            assert t1 == pytest.approx(c["t1"], rel=1e-6, abs=1e-30), c
+    for c in g["distance"]:
+        ray = o.ray_normalize(np.asarray(c["ray"], np.float32))[0]
+        want = np.inf if c["distance"] == "inf" else c["distance"]
+        assert o.ray_box_distance(ray, box) == want
+
+
+def test_oracle_ray_tree_cases_golden(golden):
+    """test/tstQueryTreeRay.cpp:62-265 through the brute-force restatement."""
+    g = golden["rays"]
+    boxes = np.asarray(g["tree_boxes"], np.float32)
+    r = o.ray_normalize(np.asarray([g["tree_intersects"]["ray"]], np.float32))
+    off, ind, _ = o.ray_brute(boxes, r, ordered=False)
+    assert ind.tolist() == g["tree_intersects"]["indices"]
+    for c in g["tree_ordered"]:
+        off, ind, _ = o.ray_brute(boxes, o.ray_normalize(np.asarray([c["ray"]], np.float32)), ordered=True)
+        assert ind.tolist() == c["indices"]
+    one = g["single_leaf"]
+    off, ind, _ = o.ray_brute(np.asarray([one["box"]], np.float32),
+                              o.ray_normalize(np.asarray(one["rays"], np.float32)), ordered=True)
+    assert off.tolist() == one["offsets"] and ind.tolist() == one["indices"]
