@@ -12,7 +12,7 @@ All compute runs in libarborx_gb300.so; tensors are passed as raw device
 pointers and results are zero-copy views of the library's own buffers.
 """
 
-from ._lib import AbxError, SearchException  # noqa: F401
+from ._lib import BOX, POINT, RAY, SPHERE, AbxError, SearchException  # noqa: F401
 from .serve import Server  # noqa: F401
 from .bvh import (  # noqa: F401
     BoundingVolumeHierarchy,
@@ -33,6 +33,8 @@ from .bvh import (  # noqa: F401
     morton32,
     morton64,
     nearest,
+    ordered_intersects,
+    ray_intersects,
     query,
     query_nearest_into,
     scene_bounds,

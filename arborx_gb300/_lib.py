@@ -21,7 +21,7 @@ ERROR_NOT_SUPPORTED = 6
 ERROR_TIMEOUT = 7
 
 # abx_geometry
-POINT, BOX, SPHERE = 0, 1, 2
+POINT, BOX, SPHERE, RAY = 0, 1, 2, 3
 
 # Every function the header declares: name -> (restype, argtypes)
 _P = ctypes.c_void_p
@@ -123,6 +123,9 @@ SIGNATURES = {
     "abx_server_result": (_STATUS, [_P, _I64, _P, _P, _P]),
     "abx_server_stats": (_STATUS, [_P, ctypes.POINTER(ServerStatisticsC)]),
     "abx_server_reset_stats": (_STATUS, [_P]),
+    "abx_bvh_query_ordered_intersects": (
+        _STATUS, [_P, _P, _P, _I64, _I32, TraversalPolicyC, _I32, ctypes.POINTER(_P)],
+    ),
     "abx_bvh_query_nearest_into": (
         _STATUS, [_P, _P, _P, _I64, _I32, TraversalPolicyC, _P, _P, _P],
     ),

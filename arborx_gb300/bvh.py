@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import BOX, POINT, SPHERE, TraversalPolicyC, check
+from ._lib import BOX, POINT, RAY, SPHERE, TraversalPolicyC, check
 
 
 def version():
@@ -110,6 +110,29 @@ class Intersects:
 
     def __len__(self):
         return self.data.shape[0]
+
+
+class OrderedIntersects:
+    """Batch of Experimental::ordered_intersects(Ray) predicates
+    (ArborX_Predicates.hpp:103-125): rays [nq, 6] (origin xyz, direction
+    xyz; the library normalizes the direction as the Ray constructor does).
+    k > 0 keeps the first k hits per ray (nearest(Ray, k))."""
+
+    def __init__(self, rays, k=0):
+        self.data = _as_rows(rays, 6, "rays")
+        self.k = int(k)
+
+    def __len__(self):
+        return self.data.shape[0]
+
+
+def ordered_intersects(rays, k=0):
+    return OrderedIntersects(rays, k)
+
+
+def ray_intersects(rays):
+    """intersects(Ray) for every row of rays [nq, 6]."""
+    return Intersects(rays, RAY)
 
 
 class Nearest:
@@ -288,8 +311,15 @@ def query(tree, predicates, policy=None, space=None, with_distances=False):
                 kv, policy._c(), 1 if with_distances else 0, ctypes.byref(h),
             )
         )
+    elif isinstance(predicates, OrderedIntersects):
+        if prefix != "abx_bvh":
+            raise TypeError("ordered_intersects: tree queries only")
+        check(L.abx_bvh_query_ordered_intersects(
+            tree._h, s, _ptr(predicates.data), len(predicates), predicates.k, policy._c(),
+            1 if with_distances else 0, ctypes.byref(h)))
+        return _crs_result(h, with_distances)
     else:
-        raise TypeError("predicates must be Intersects or Nearest")
+        raise TypeError("predicates must be Intersects, Nearest or OrderedIntersects")
     return _crs_result(h, isinstance(predicates, Nearest) and with_distances)
 
 

@@ -314,6 +314,8 @@ abx_status morton32_codes(cudaStream_t s, abx_geometry kind, const float *d_g, i
     k_morton32<1><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
   else if (kind == ABX_SPHERE)
     k_morton32<2><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
+  else if (kind == ABX_RAY)
+    k_morton32<3><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
 }

@@ -140,11 +140,23 @@ abx_status launch_spatial_self(cudaStream_t s, TreeView const &t, int filter,
 // a half list (row i = its half row, then the rows k listing i, ascending k).
 abx_status self_spheres(cudaStream_t s, const float *d_points, int64_t n, float r,
                         float *d_spheres);
-abx_status leaf_order(cudaStream_t s, const float4 *d_sorted, int64_t n, uint32_t *d_order,
-                      int32_t *d_pos);
+abx_status leaf_order(cudaStream_t s, abx_geometry kind, const float4 *d_sorted, int64_t n,
+                      uint32_t *d_order, int32_t *d_pos);
 abx_status expand_half_to_full(cudaStream_t s, int64_t n, const int32_t *d_half_off,
                                const int32_t *d_half_idx, int64_t m, int32_t *d_full_off,
                                int32_t *d_full_idx);
+
+// Rays: Ray{origin, direction} construction (direction normalized in
+// double); the ordering pass of ordered_intersects: the m results of a ray
+// CRS (d_offsets, d_indices) sorted per ray by (distance, value), at most k
+// per ray (k <= 0: all), into d_new_offsets (nq + 1) and d_out_idx /
+// d_out_dist (room for m); the kept total in *h_new_total (synchronises s).
+abx_status ray_normalize(cudaStream_t s, const float *d_raw, int64_t n, float *d_out);
+abx_status order_ray_results(cudaStream_t s, abx_geometry leaf_kind, const float4 *d_sorted,
+                             int64_t n, const float *d_rays, int64_t nq, const int32_t *d_offsets,
+                             const int32_t *d_indices, int64_t m, int32_t k,
+                             int32_t *d_new_offsets, int32_t *d_out_idx, float *d_out_dist,
+                             int64_t *h_new_total);
 
 // The queries whose result count (from CRS offsets) exceeds `buffer`, into
 // d_list (nq entries of room); their number in *h_count (synchronises s).

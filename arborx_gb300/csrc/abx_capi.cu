@@ -825,14 +825,23 @@ abx_status abx_bvh_query_intersects(const abx_bvh *bvh, void *stream, abx_geomet
   *out = nullptr;
   if (bvh->d_off)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: a forest handle");
-  if (kind != ABX_SPHERE && kind != ABX_BOX)
+  if (kind != ABX_SPHERE && kind != ABX_BOX && kind != ABX_RAY)
     return fail(ABX_ERROR_INVALID_ARGUMENT,
-                "abx_bvh_query_intersects: predicates must be spheres or boxes");
+                "abx_bvh_query_intersects: predicates must be spheres, boxes or rays");
   if (nq < 0 || nq >= (int64_t)INT32_MAX)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: bad number of queries");
   if (nq > 0 && !d_predicates)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: null predicates");
-  return query_intersects(bvh, as_stream(stream), kind, d_predicates, nq, nullptr, policy, out);
+  cudaStream_t s = as_stream(stream);
+  if (kind == ABX_RAY)
+  {
+    device_state();
+    Scratch<float> rays;
+    ABX_CUDA_TRY(rays.alloc((size_t)std::max<int64_t>(nq, 1) * 6, s));
+    ABX_TRY(ray_normalize(s, d_predicates, nq, rays.ptr));
+    return query_intersects(bvh, s, kind, rays.ptr, nq, nullptr, policy, out);
+  }
+  return query_intersects(bvh, s, kind, d_predicates, nq, nullptr, policy, out);
 }
 
 abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream, const float *d_queries,
@@ -891,6 +900,54 @@ abx_status abx_bvh_query_nearest_into(const abx_bvh *bvh, void *stream, const fl
   }
   return launch_nearest(s, view_of(bvh), nullptr, d_queries, nq, perm.ptr, nullptr, k, k, nullptr,
                         d_offsets, d_indices, dist);
+}
+
+abx_status abx_bvh_query_ordered_intersects(const abx_bvh *bvh, void *stream, const float *d_rays,
+                                            int64_t nq, int32_t k, abx_traversal_policy policy,
+                                            int32_t with_distances, abx_crs **out)
+{
+  if (!bvh || !out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_ordered_intersects: null argument");
+  *out = nullptr;
+  if (bvh->d_off)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_ordered_intersects: a forest handle");
+  if (nq < 0 || nq >= (int64_t)INT32_MAX || (nq > 0 && !d_rays))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_ordered_intersects: bad rays");
+  cudaStream_t s = as_stream(stream);
+  device_state();
+  Scratch<float> rays;
+  ABX_CUDA_TRY(rays.alloc((size_t)std::max<int64_t>(nq, 1) * 6, s));
+  ABX_TRY(ray_normalize(s, d_rays, nq, rays.ptr));
+  abx_crs *raw = nullptr;
+  ABX_TRY(query_intersects(bvh, s, ABX_RAY, rays.ptr, nq, nullptr, policy, &raw));
+  std::unique_ptr<abx_crs, void (*)(abx_crs *)> hits(raw, destroy_crs);
+  abx_crs *c = new (std::nothrow) abx_crs;
+  if (!c)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
+  cudaGetDevice(&c->device);
+  c->stream = s;
+  c->nq = nq;
+  auto bail = [&](abx_status st) {
+    cudaStreamSynchronize(s);
+    destroy_crs(c);
+    return st;
+  };
+  const int64_t m = raw->nres;
+  if (dmalloc_n(&c->offsets, nq + 1, s) != cudaSuccess ||
+      dmalloc_n(&c->indices, (size_t)m, s) != cudaSuccess ||
+      (with_distances && dmalloc_n(&c->distances, (size_t)m, s) != cudaSuccess))
+    return bail(fail(ABX_ERROR_OUT_OF_MEMORY, "CRS"));
+  if (nq == 0)
+    cudaMemsetAsync(c->offsets, 0, sizeof(int32_t), s);
+  int64_t total = 0;
+  abx_status st = order_ray_results(s, bvh->kind, bvh->sorted, bvh->n, rays.ptr, nq, raw->offsets,
+                                    raw->indices, m, k, c->offsets, c->indices, c->distances,
+                                    &total);
+  if (st != ABX_SUCCESS)
+    return bail(st);
+  c->nres = total;
+  *out = c;
+  return ABX_SUCCESS;
 }
 
 abx_status abx_forest_create(void *stream, abx_geometry kind, const float *d_values,
@@ -1172,7 +1229,7 @@ abx_status abx_find_neighbor_list(void *stream, const float *d_points, int64_t n
   // queries in the tree's leaf order: Morton-coherent without a sort
   abx_status st = self_spheres(s, d_points, n, radius, spheres.ptr);
   if (st == ABX_SUCCESS)
-    st = leaf_order(s, t->sorted, n, order.ptr, pos.ptr);
+    st = leaf_order(s, t->kind, t->sorted, n, order.ptr, pos.ptr);
   const TreeView tv = view_of(t);
   const int filter = half ? 2 : 1;
   if (st == ABX_SUCCESS)

@@ -301,6 +301,65 @@ __device__ __forceinline__ void load_centroid<2>(const float *g, int64_t i,
   z = __ldg(g + 4 * i + 2);
 }
 
+// A ray's centroid is its origin (returnCentroid, ArborX_Ray.hpp:78-82).
+template <>
+__device__ __forceinline__ void load_centroid<3>(const float *g, int64_t i,
+                                                 float &x, float &y, float &z)
+{
+  x = __ldg(g + 6 * i);
+  y = __ldg(g + 6 * i + 1);
+  z = __ldg(g + 6 * i + 2);
+}
+
+// intersection(Ray, Box, tmin, tmax) (ArborX_Ray.hpp:107-158): slab test of
+// a ray (origin o, normalized direction d) with a zero direction component
+// handled through signs; the comparisons never let a NaN update the bounds.
+__device__ __forceinline__ bool ray_box_intersection(float const (&o)[3], float const (&d)[3],
+                                                     Box3 const &b, float &tmin, float &tmax)
+{
+  tmin = -INFINITY;
+  tmax = INFINITY;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+  {
+    float tdmin, tdmax;
+    if (d[k] == 0.f)
+    {
+      const float min_orig = __fsub_rn(b.lo[k], o[k]);
+      if (min_orig == 0.f)
+        continue;
+      const float max_orig = __fsub_rn(b.hi[k], o[k]);
+      tdmin = signbit(__fmul_rn(d[k], max_orig)) ? INFINITY : -INFINITY;
+      tdmax = signbit(__fmul_rn(d[k], min_orig)) ? INFINITY : -INFINITY;
+    }
+    else if (d[k] > 0.f)
+    {
+      tdmin = __fdiv_rn(__fsub_rn(b.lo[k], o[k]), d[k]);
+      tdmax = __fdiv_rn(__fsub_rn(b.hi[k], o[k]), d[k]);
+    }
+    else
+    {
+      tdmin = __fdiv_rn(__fsub_rn(b.hi[k], o[k]), d[k]);
+      tdmax = __fdiv_rn(__fsub_rn(b.lo[k], o[k]), d[k]);
+    }
+    if (tmin < tdmin)
+      tmin = tdmin;
+    if (tmax > tdmax)
+      tmax = tdmax;
+  }
+  return tmin <= tmax;
+}
+
+// distance(Ray, Box) (ArborX_Ray.hpp:435-447): entry distance max(tmin, 0)
+// of a box in front of the ray, +inf otherwise.
+__device__ __forceinline__ float ray_box_distance(float const (&o)[3], float const (&d)[3],
+                                                  Box3 const &b)
+{
+  float t0, t1;
+  const bool hit = ray_box_intersection(o, d, b, t0, t1) && t1 >= 0.f;
+  return hit ? (t0 < 0.f ? 0.f : t0) : INFINITY;
+}
+
 // Bounding box of a leaf value: expand(empty, indexable).
 template <int KIND>
 __device__ __forceinline__ Box3 load_leaf_box(const float *g, int64_t i)

@@ -20,16 +20,21 @@ __global__ void k_self_spheres(const float *__restrict__ pts, int64_t n, float r
 }
 
 // The tree's leaf order: order[t] = value of the leaf at Morton position t,
-// pos[value] = t.
+// pos[value] = t (a box leaf spans two float4, its value in the first).
+template <int KIND>
 __global__ void k_leaf_order(const float4 *__restrict__ sorted, int64_t n,
-                             uint32_t *__restrict__ order, int32_t *__restrict__ pos)
+                             uint32_t *__restrict__ order, int32_t *__restrict__ pos,
+                             unsigned *__restrict__ err)
 {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n)
     return;
-  const int v = __float_as_int(sorted[t].w);
+  const int v = __float_as_int(sorted[KIND == 1 ? 2 * t : t].w);
   order[t] = (uint32_t)v;
-  pos[v] = (int32_t)t;
+  if ((uint64_t)v < (uint64_t)n)
+    pos[v] = (int32_t)t;
+  else
+    raise_error(err, ABX_DEVERR_INTERNAL);
 }
 
 // Mirrored pairs of a half list: entry j of row k (value i) gives the pair
@@ -94,12 +99,17 @@ abx_status self_spheres(cudaStream_t s, const float *d_points, int64_t n, float 
   return ABX_SUCCESS;
 }
 
-abx_status leaf_order(cudaStream_t s, const float4 *d_sorted, int64_t n, uint32_t *d_order,
-                      int32_t *d_pos)
+abx_status leaf_order(cudaStream_t s, abx_geometry kind, const float4 *d_sorted, int64_t n,
+                      uint32_t *d_order, int32_t *d_pos)
 {
   if (n <= 0)
     return ABX_SUCCESS;
-  k_leaf_order<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_sorted, n, d_order, d_pos);
+  unsigned *err = device_state().d_error;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  if (kind == ABX_BOX)
+    k_leaf_order<1><<<blocks, 256, 0, s>>>(d_sorted, n, d_order, d_pos, err);
+  else
+    k_leaf_order<0><<<blocks, 256, 0, s>>>(d_sorted, n, d_order, d_pos, err);
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
 }

@@ -122,8 +122,41 @@ struct BoxPred
   }
 };
 
+// intersects(Ray, .): the box in front of the ray (ArborX_Ray.hpp:160-168);
+// point leaves are degenerate boxes.  Rows hold the normalized ray.
+struct RayPred
+{
+  float o[3], d[3];
+  __device__ __forceinline__ bool test(Box3 const &b) const
+  {
+    float t0, t1;
+    return ray_box_intersection(o, d, b, t0, t1) && t1 >= 0.f;
+  }
+  template <int KIND>
+  __device__ __forceinline__ bool test_leaf(Box3 const &b) const
+  {
+    return test(b);
+  }
+};
+
 template <int PRED>
 struct PredOf;
+template <>
+struct PredOf<ABX_RAY>
+{
+  static __device__ __forceinline__ RayPred load(const float *p, int64_t q)
+  {
+    const float *r = p + 6 * q;
+    RayPred rp;
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+      rp.o[k] = __ldg(r + k);
+      rp.d[k] = __ldg(r + 3 + k);
+    }
+    return rp;
+  }
+};
 template <>
 struct PredOf<ABX_SPHERE>
 {
@@ -1164,7 +1197,12 @@ abx_status launch_spatial(cudaStream_t s, TreeView const &t, ForestView const *f
                                                      d_offsets, d_out, buffer, d_overflow)
                       : spatial_dispatch<ABX_BOX, 0>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
                                                      d_offsets, d_out, buffer, d_overflow);
-  return fail(ABX_ERROR_INVALID_ARGUMENT, "intersects predicates must be spheres or boxes");
+  if (pred_kind == ABX_RAY)
+    return box_leaves ? spatial_dispatch<ABX_RAY, 1>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
+                                                     d_offsets, d_out, buffer, d_overflow)
+                      : spatial_dispatch<ABX_RAY, 0>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
+                                                     d_offsets, d_out, buffer, d_overflow);
+  return fail(ABX_ERROR_INVALID_ARGUMENT, "intersects predicates must be spheres, boxes or rays");
 }
 
 abx_status brute_pack(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,

@@ -58,13 +58,17 @@ typedef struct abx_brute abx_brute;   /* opaque brute-force index             */
  *   POINT  x y z                 (12 bytes)   ArborX::Point<3>
  *   BOX    minx miny minz maxx maxy maxz (24) ArborX::Box<3>
  *   SPHERE cx cy cz r            (16 bytes)   ArborX::Sphere<3>
+ *   RAY    ox oy oz dx dy dz     (24 bytes)   ArborX::Experimental::Ray<float>
+ *          (predicates only; the direction is normalized by the library as
+ *          the Ray constructor does, ArborX_Ray.hpp:46-55)
  * (src/geometry/ArborX_Point.hpp:24-38, ArborX_Box.hpp:32-67,
- *  ArborX_Sphere.hpp:25-47). */
+ *  ArborX_Sphere.hpp:25-47, ArborX_Ray.hpp:33-66). */
 typedef enum abx_geometry
 {
   ABX_POINT = 0,
   ABX_BOX = 1,
-  ABX_SPHERE = 2
+  ABX_SPHERE = 2,
+  ABX_RAY = 3
 } abx_geometry;
 
 /* TraversalPolicy (src/spatial/detail/ArborX_TraversalPolicy.hpp:19-47):
@@ -386,6 +390,19 @@ ABX_API abx_status abx_server_result(abx_server *srv, int64_t ticket, int32_t *h
                                      int32_t *h_indices, float *h_distances);
 ABX_API abx_status abx_server_stats(abx_server *srv, abx_server_statistics *out);
 ABX_API abx_status abx_server_reset_stats(abx_server *srv);
+
+/* ordered_intersects(Ray) (Experimental::OrderedSpatial,
+ * ArborX_Predicates.hpp:103-125; traversal ArborX_TreeTraversal.hpp:338-489):
+ * per ray, the leaves in front of it by increasing distance(Ray, Box)
+ * (ArborX_Ray.hpp:435-447, the entry distance), equal distances by value
+ * (the reference reports them in heap order).  k > 0 keeps the first k per
+ * ray, which is nearest(Ray, k) (leaves the ray misses are never
+ * candidates).  d_rays: nq rows of ABX_RAY.  with_distances keeps the
+ * distances (abx_crs_distances).  Synchronises the stream. */
+ABX_API abx_status abx_bvh_query_ordered_intersects(const abx_bvh *bvh, void *stream,
+                                                    const float *d_rays, int64_t nq, int32_t k,
+                                                    abx_traversal_policy policy,
+                                                    int32_t with_distances, abx_crs **out);
 
 /* nearest(point, k) with one k for all queries into caller-provided device
  * arrays and no host synchronisation, so that the call can be captured in a
