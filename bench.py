@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1_000_000,
                     help="queries timed per CPU step (scaled to --nq)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-vs-plain measurement in the headline line")
     ap.add_argument("--dist", default="uniform", choices=["uniform", "clustered"],
                     help="--case build/nearest/radius: point distribution")
     ap.add_argument("--serve-requests", type=int, default=2000)
@@ -201,7 +203,7 @@ def pci_bus_id(torch, dev):
 # ---------------------------------------------------------------------------
 
 
-def cpu_step(points, queries, k, sample):
+def cpu_step(points, queries, k, sample, keep_tree=False):
     from oracle import oracle as orc
 
     t0 = time.perf_counter()
@@ -211,20 +213,34 @@ def cpu_step(points, queries, k, sample):
     tree.nearest(queries[:m], k, mode=orc.MODE_ARBORX)
     t2 = time.perf_counter()
     scale = len(queries) / m
+    if keep_tree:
+        return (t1 - t0), (t2 - t1) * scale, tree
     return (t1 - t0), (t2 - t1) * scale
 
 
-def cpu_baseline(points, queries, k, sample, steps=1):
+def cpu_baseline(points, queries, k, sample, steps=1, gpu_indices=None, check=2000):
+    """The oracle on the host cores (bounded sample), and, when the GPU's
+    result indices of the same workload are given (uniform k, query order),
+    a bit-exact comparison of the first `check` queries with the oracle's
+    (distance, index) rule."""
     from oracle import oracle as orc
 
     threads = orc.num_threads()
     best = None
+    tree = None
     for _ in range(steps):
-        tb, tq = cpu_step(points, queries, k, sample)
+        tb, tq, tree = cpu_step(points, queries, k, sample, keep_tree=True)
         if best is None or tb + tq < best[0] + best[1]:
             best = (tb, tq)
     tb, tq = best
-    return {
+    parity = None
+    if gpu_indices is not None:
+        m = min(check, len(queries))
+        _, ref_idx, _ = tree.nearest(queries[:m], k, mode=orc.MODE_ORDERED)
+        got = np.asarray(gpu_indices[: m * min(k, len(points))])
+        parity = {"queries_checked": int(m), "bit_exact": bool(np.array_equal(got, ref_idx)),
+                  "rule": "k smallest (distance, index), oracle restatement"}
+    out = {
         "value": len(queries) / (tb + tq),
         "unit": "queries/s",
         "cores": threads,
@@ -233,6 +249,9 @@ def cpu_baseline(points, queries, k, sample, steps=1):
         % (len(points), k, min(sample, len(queries)), len(queries)),
         "build_mpts_per_s": len(points) / tb / 1e6,
     }
+    if parity is not None:
+        out["parity"] = parity
+    return out
 
 
 def run_reference(args):
@@ -485,8 +504,15 @@ def run_gpu(args):
             "clocks": clk,
         }
         if world == 1 and not args.no_cpu_baseline:
-            cpu = cpu_baseline(points_np, queries_np, args.k, args.cpu_sample)
+            cpu = cpu_baseline(points_np, queries_np, args.k, args.cpu_sample,
+                               gpu_indices=out_idx_h.numpy())
+            line["parity"] = cpu.pop("parity", None)
             line["cpu_baseline"] = cpu
+        if world == 1 and not args.no_batched:
+            try:
+                line["batched"] = measure_forest(args.clouds, warmup=2, steps=3, plain_steps=1)
+            except Exception as e:  # reported, never fatal for the headline line
+                line["batched"] = {"error": str(e)[:200]}
         print(json.dumps(line), flush=True)
     group.barrier()
     group.close()
@@ -571,7 +597,7 @@ def make_clouds(ncl):
     return pts, boxes, offsets
 
 
-def run_forest(args):
+def measure_forest(clouds, warmup=2, steps=3, plain_steps=1):
     """Batched vs plain on the many-clouds workload: one Forest build + one
     forest box query, against the per-tree loop (one BVH build and one query
     per cloud on one stream, the reference's many-trees pattern,
@@ -582,10 +608,8 @@ def run_forest(args):
     import torch
 
     import arborx_gb300 as ax
-    from arborx_gb300 import build as libbuild
 
-    libbuild.build()
-    pts_np, boxes_np, off = make_clouds(args.clouds)
+    pts_np, boxes_np, off = make_clouds(clouds)
     pts = torch.from_numpy(pts_np).cuda()
     boxes = torch.from_numpy(boxes_np).cuda()
     ntrees = off.size - 1
@@ -601,19 +625,19 @@ def run_forest(args):
             out.append(ax.query(ax.BoundingVolumeHierarchy(p), ax.intersects(b)))
         return out
 
-    def timed(fn, steps):
+    def timed(fn, n):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(steps):
+        for _ in range(n):
             r = fn()
         torch.cuda.synchronize()
-        return (time.perf_counter() - t0) / steps, r
+        return (time.perf_counter() - t0) / n, r
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batched()
-    tb, (bi, bo) = timed(batched, args.steps)
+    tb, (bi, bo) = timed(batched, steps)
     plain()
-    tp, per = timed(plain, max(1, min(args.steps, 3)))
+    tp, per = timed(plain, plain_steps)
     bo_h = bo.cpu().numpy()
     bi_h = bi.cpu().numpy()
     same = True
@@ -624,14 +648,24 @@ def run_forest(args):
             same = False
             break
     total = int(off[-1])
-    print(json.dumps({
-        "case": "forest", "clouds": ntrees, "points": total, "queries": total,
+    return {
+        "workload": "%d clouds of floor(10^U(2,5)) points, %d points, one box query per point"
+        % (ntrees, total),
         "results": int(bo_h[-1]),
         "batched_ms": tb * 1e3, "plain_ms": tp * 1e3, "speedup": tp / tb,
         "batched_points_per_s": total / tb, "plain_points_per_s": total / tp,
         "bit_exact": same,
-    }), flush=True)
-    if not same:
+    }
+
+
+def run_forest(args):
+    from arborx_gb300 import build as libbuild
+
+    libbuild.build()
+    res = measure_forest(args.clouds, args.warmup, args.steps, max(1, min(args.steps, 3)))
+    res["case"] = "forest"
+    print(json.dumps(res), flush=True)
+    if not res["bit_exact"]:
         sys.exit(1)
 
 
