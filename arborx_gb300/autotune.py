@@ -21,7 +21,7 @@ from . import _lib
 KNOBS = {
     "NEAREST_BUCKET": [1, 2, 4, 8, 16],
     "SPATIAL_BUCKET": [1, 4, 8, 16, 32],
-    "SORT_TOP_PASSES": [0, 3],
+    "SORT_TOP_PASSES": [0, 3, 4],
 }
 DEFAULTS = {"NEAREST_BUCKET": 1, "SPATIAL_BUCKET": 8, "SORT_TOP_PASSES": 3}
 

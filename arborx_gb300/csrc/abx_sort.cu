@@ -322,8 +322,8 @@ __device__ __forceinline__ void run_bounds(const K *__restrict__ keys, int64_t n
 // most kRunMax equal top-bit keys at its rank by (key, position), which is the
 // stable order; keys of longer runs are copied in place and counted.  A CTA
 // stages its keys with a halo of kFixHalo on each side in shared memory,
-// with the top bits as 32-bit words (fewer than 32 bits remain above any
-// shift used here) and sentinels past both ends of the array.
+// with the top bits (key >> shift, shift >= 8, so never all ones) and two
+// all-ones sentinels past both ends of the array.
 constexpr int kFixThreads = 256;
 constexpr int kFixHalo = kRunMax + 2;
 
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(kFixThreads)
 {
   constexpr int kSpan = kFixThreads + 2 * kFixHalo;
   __shared__ K s_key[kSpan];
-  __shared__ uint32_t s_top[kSpan];
+  __shared__ K s_top[kSpan];
   const int64_t b = (int64_t)blockIdx.x * kFixThreads;
   for (int j = threadIdx.x; j < kSpan; j += kFixThreads)
   {
@@ -343,8 +343,8 @@ __global__ void __launch_bounds__(kFixThreads)
     const bool in = g >= 0 && g < n;
     const K k = in ? kin[g] : (K)0;
     s_key[j] = k;
-    // tops are below 2^24; the two sentinels differ from them and each other
-    s_top[j] = in ? (uint32_t)(k >> shift) : (g < 0 ? 0xffffffffu : 0xfffffffeu);
+    // a top is below 2^(bits - 8); the sentinels differ from it and each other
+    s_top[j] = in ? (K)(k >> shift) : (g < 0 ? ~(K)0 : ~(K)1);
   }
   __syncthreads();
   const int64_t i = b + threadIdx.x;
@@ -352,7 +352,7 @@ __global__ void __launch_bounds__(kFixThreads)
   if (i < n)
   {
     const int li = threadIdx.x + kFixHalo;
-    const uint32_t top = s_top[li];
+    const K top = s_top[li];
     int a = li;
     while (li - a <= kRunMax && s_top[a - 1] == top)
       --a;
@@ -600,8 +600,6 @@ abx_status radix_sort_impl(cudaStream_t s, K *d_keys, uint32_t *d_vals,
     return fail(ABX_ERROR_INVALID_ARGUMENT, "radix sort: bad number of passes");
   if (top < 0 || top >= num_passes)
     top = 0;
-  // the fix-up keeps the top bits in 32-bit words with two reserved values
-  top = std::min(top, 3);
   StageScope scope(s, sizeof(K) == 8 ? "sort64" : "sort32", 0);
   int launches = 0;
   abx_status st = top > 0
@@ -771,11 +769,12 @@ abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
 
 int hybrid_top_passes(int64_t n, int num_passes)
 {
-  // 3 top digits (24 bits) spread up to ~2^24 keys into short runs; below
-  // 2^16 keys the plain sort is as cheap
+  // 3 top digits (24 bits) spread up to ~2^24 keys into short runs, 4 digits
+  // up to ~2^32; below 2^16 keys the plain sort is as cheap
   if (n < (1 << 16) || num_passes <= 3)
     return 0;
-  return tuning_value("SORT_TOP_PASSES", 3);
+  const int def = n <= (int64_t)(1 << 24) ? 3 : 4;
+  return std::min(tuning_value("SORT_TOP_PASSES", def), num_passes - 1);
 }
 
 abx_status exclusive_scan_i32(cudaStream_t s, const int32_t *d_in, int64_t n, int32_t *d_out)

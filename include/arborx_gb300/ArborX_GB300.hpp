@@ -37,6 +37,9 @@ public:
   explicit SearchException(std::string const &msg) : std::logic_error(msg) {}
 };
 
+template <class T>
+class DeviceView;
+
 namespace Details
 {
 inline void check(abx_status s)
@@ -84,7 +87,21 @@ struct Sphere
   __host__ __device__ float radius() const { return r; }
 };
 
-static_assert(sizeof(Point) == 12 && sizeof(Box) == 24 && sizeof(Sphere) == 16,
+namespace Experimental
+{
+// ArborX::Experimental::Ray (src/geometry/ArborX_Ray.hpp:33-66).  The
+// direction is stored as given; the library normalizes it (in double, as
+// the reference's constructor does) when it runs a query.
+struct Ray
+{
+  Point origin;
+  Point direction;
+  __host__ __device__ Point const &origin_point() const { return origin; }
+};
+} // namespace Experimental
+
+static_assert(sizeof(Point) == 12 && sizeof(Box) == 24 && sizeof(Sphere) == 16 &&
+                  sizeof(Experimental::Ray) == 24,
               "geometry rows must match the C ABI");
 
 // A device array owning its memory: the counterpart of
@@ -135,6 +152,51 @@ private:
   size_t _size = 0;
 };
 
+namespace Details
+{
+// Move a CRS result of the library into the caller's arrays (the reference
+// reallocates indices and offsets in the callee,
+// ArborX_CrsGraphWrapperImpl.hpp:376-377).
+inline void take(cudaStream_t space, abx_crs *crs, int64_t nq, DeviceView<int> &indices,
+                 DeviceView<int> &offsets, DeviceView<float> *distances)
+{
+  std::unique_ptr<abx_crs, abx_status (*)(abx_crs *)> guard(crs, abx_crs_destroy);
+  const int64_t nres = abx_crs_num_results(crs);
+  offsets.realloc((size_t)nq + 1);
+  indices.realloc((size_t)nres);
+  check_cuda(cudaMemcpyAsync(offsets.data(), abx_crs_offsets(crs), (nq + 1) * sizeof(int),
+                             cudaMemcpyDeviceToDevice, space));
+  if (nres)
+    check_cuda(cudaMemcpyAsync(indices.data(), abx_crs_indices(crs), nres * sizeof(int),
+                               cudaMemcpyDeviceToDevice, space));
+  if (distances)
+  {
+    distances->realloc((size_t)nres);
+    if (nres)
+      check_cuda(cudaMemcpyAsync(distances->data(), abx_crs_distances(crs), nres * sizeof(float),
+                                 cudaMemcpyDeviceToDevice, space));
+  }
+  // the result's arrays are released stream-ordered after the copies
+}
+
+template <class Policy>
+inline abx_traversal_policy c_policy(Policy const &p)
+{
+  return abx_traversal_policy{p._buffer_size, p._sort_predicates ? 1 : 0};
+}
+
+template <class Geometry>
+constexpr abx_geometry predicate_kind()
+{
+  if constexpr (std::is_same_v<Geometry, Sphere>)
+    return ABX_SPHERE;
+  else if constexpr (std::is_same_v<Geometry, Box>)
+    return ABX_BOX;
+  else
+    return ABX_RAY;
+}
+} // namespace Details
+
 namespace Experimental
 {
 // ArborX::Experimental::TraversalPolicy (ArborX_TraversalPolicy.hpp:19-47).
@@ -159,8 +221,9 @@ struct TraversalPolicy
 template <class Geometry>
 struct Intersects
 {
-  static_assert(std::is_same_v<Geometry, Sphere> || std::is_same_v<Geometry, Box>,
-                "intersects predicates are spheres or boxes");
+  static_assert(std::is_same_v<Geometry, Sphere> || std::is_same_v<Geometry, Box> ||
+                    std::is_same_v<Geometry, Experimental::Ray>,
+                "intersects predicates are spheres, boxes or rays");
   DeviceView<Geometry> geometries;
 };
 
@@ -186,6 +249,19 @@ inline Nearest nearest(DeviceView<Point> const &points, DeviceView<int> const &k
 
 namespace Experimental
 {
+// A batch of ordered_intersects(Ray) predicates (ArborX_Predicates.hpp:
+// 103-156): the hits of each ray by increasing distance along it; k > 0
+// keeps the first k (nearest(Ray, k)).
+struct OrderedIntersects
+{
+  DeviceView<Ray> rays;
+  int k = 0;
+};
+inline OrderedIntersects make_ordered_intersects(DeviceView<Ray> const &rays, int k = 0)
+{
+  return OrderedIntersects{rays, k};
+}
+
 // make_intersects(points, r) (ArborX_PredicateHelpers.hpp:99-105): spheres of
 // radius r around host points.
 inline Intersects<Sphere> make_intersects(std::vector<Point> const &points, float r,
@@ -236,11 +312,11 @@ public:
              Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy()) const
   {
     abx_crs *crs = nullptr;
-    constexpr abx_geometry kind = std::is_same_v<Geometry, Sphere> ? ABX_SPHERE : ABX_BOX;
+    constexpr abx_geometry kind = Details::predicate_kind<Geometry>();
     Details::check(abx_bvh_query_intersects(
         _tree.get(), space, kind, reinterpret_cast<const float *>(preds.geometries.data()),
         (int64_t)preds.geometries.size(), c_policy(policy), &crs));
-    take(space, crs, (int64_t)preds.geometries.size(), indices, offsets, nullptr);
+    Details::take(space, crs, (int64_t)preds.geometries.size(), indices, offsets, nullptr);
   }
 
   void query(cudaStream_t space, Nearest const &preds, DeviceView<int> &indices,
@@ -253,7 +329,20 @@ public:
         _tree.get(), space, reinterpret_cast<const float *>(preds.points.data()),
         (int64_t)preds.points.size(), preds.ks.size() ? preds.ks.data() : nullptr, preds.k,
         c_policy(policy), distances ? 1 : 0, &crs));
-    take(space, crs, (int64_t)preds.points.size(), indices, offsets, distances);
+    Details::take(space, crs, (int64_t)preds.points.size(), indices, offsets, distances);
+  }
+
+  // query(space, ordered_intersects(rays), indices, offsets[, policy])
+  void query(cudaStream_t space, Experimental::OrderedIntersects const &preds,
+             DeviceView<int> &indices, DeviceView<int> &offsets,
+             Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy(),
+             DeviceView<float> *distances = nullptr) const
+  {
+    abx_crs *crs = nullptr;
+    Details::check(abx_bvh_query_ordered_intersects(
+        _tree.get(), space, reinterpret_cast<const float *>(preds.rays.data()),
+        (int64_t)preds.rays.size(), preds.k, c_policy(policy), distances ? 1 : 0, &crs));
+    Details::take(space, crs, (int64_t)preds.rays.size(), indices, offsets, distances);
   }
 
   abx_bvh const *handle() const { return _tree.get(); }
@@ -267,34 +356,111 @@ private:
   }
   static abx_traversal_policy c_policy(Experimental::TraversalPolicy const &p)
   {
-    return abx_traversal_policy{p._buffer_size, p._sort_predicates ? 1 : 0};
+    return Details::c_policy(p);
   }
-  static void take(cudaStream_t space, abx_crs *crs, int64_t nq, DeviceView<int> &indices,
-                   DeviceView<int> &offsets, DeviceView<float> *distances)
-  {
-    std::unique_ptr<abx_crs, abx_status (*)(abx_crs *)> guard(crs, abx_crs_destroy);
-    const int64_t nres = abx_crs_num_results(crs);
-    offsets.realloc((size_t)nq + 1);
-    indices.realloc((size_t)nres);
-    Details::check_cuda(cudaMemcpyAsync(offsets.data(), abx_crs_offsets(crs),
-                                        (nq + 1) * sizeof(int), cudaMemcpyDeviceToDevice, space));
-    if (nres)
-      Details::check_cuda(cudaMemcpyAsync(indices.data(), abx_crs_indices(crs),
-                                          nres * sizeof(int), cudaMemcpyDeviceToDevice, space));
-    if (distances)
-    {
-      distances->realloc((size_t)nres);
-      if (nres)
-        Details::check_cuda(cudaMemcpyAsync(distances->data(), abx_crs_distances(crs),
-                                            nres * sizeof(float), cudaMemcpyDeviceToDevice,
-                                            space));
-    }
-  }
-
   std::shared_ptr<abx_bvh> _tree;
 };
 
 using BVH = BoundingVolumeHierarchy;
+
+// ArborX::BruteForce (src/spatial/ArborX_BruteForce.hpp:40-176): every
+// predicate against every value; the same query interface.
+class BruteForce
+{
+public:
+  using size_type = int64_t;
+  using bounding_volume_type = Box;
+  using value_type = int;
+
+  BruteForce(cudaStream_t space, DeviceView<Point> const &points)
+  {
+    create(space, ABX_POINT, reinterpret_cast<const float *>(points.data()),
+           (int64_t)points.size());
+  }
+  BruteForce(cudaStream_t space, DeviceView<Box> const &boxes)
+  {
+    create(space, ABX_BOX, reinterpret_cast<const float *>(boxes.data()), (int64_t)boxes.size());
+  }
+  size_type size() const noexcept { return abx_brute_size(_index.get()); }
+  bool empty() const noexcept { return size() == 0; }
+  Box bounds() const
+  {
+    float b[6];
+    Details::check(abx_brute_bounds(_index.get(), b));
+    return Box(Point{{b[0], b[1], b[2]}}, Point{{b[3], b[4], b[5]}});
+  }
+  template <class Geometry>
+  void query(cudaStream_t space, Intersects<Geometry> const &preds, DeviceView<int> &indices,
+             DeviceView<int> &offsets,
+             Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy()) const
+  {
+    abx_crs *crs = nullptr;
+    Details::check(abx_brute_query_intersects(
+        _index.get(), space, Details::predicate_kind<Geometry>(),
+        reinterpret_cast<const float *>(preds.geometries.data()), (int64_t)preds.geometries.size(),
+        Details::c_policy(policy), &crs));
+    Details::take(space, crs, (int64_t)preds.geometries.size(), indices, offsets, nullptr);
+  }
+  void query(cudaStream_t space, Nearest const &preds, DeviceView<int> &indices,
+             DeviceView<int> &offsets,
+             Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy(),
+             DeviceView<float> *distances = nullptr) const
+  {
+    abx_crs *crs = nullptr;
+    Details::check(abx_brute_query_nearest(
+        _index.get(), space, reinterpret_cast<const float *>(preds.points.data()),
+        (int64_t)preds.points.size(), preds.ks.size() ? preds.ks.data() : nullptr, preds.k,
+        Details::c_policy(policy), distances ? 1 : 0, &crs));
+    Details::take(space, crs, (int64_t)preds.points.size(), indices, offsets, distances);
+  }
+
+private:
+  void create(cudaStream_t space, abx_geometry kind, const float *values, int64_t n)
+  {
+    abx_brute *b = nullptr;
+    Details::check(abx_brute_create(space, kind, values, n, &b));
+    _index.reset(b, [](abx_brute *p) { abx_brute_destroy(p); });
+  }
+  std::shared_ptr<abx_brute> _index;
+};
+
+namespace Experimental
+{
+// findFullNeighborList / findHalfNeighborList (src/spatial/detail/
+// ArborX_NeighborList.hpp:47-188): the radius self-join of the points.
+inline void findFullNeighborList(cudaStream_t space, DeviceView<Point> const &points, float radius,
+                                 DeviceView<int> &offsets, DeviceView<int> &indices)
+{
+  abx_crs *crs = nullptr;
+  Details::check(abx_find_neighbor_list(space, reinterpret_cast<const float *>(points.data()),
+                                        (int64_t)points.size(), radius, 0, &crs));
+  Details::take(space, crs, (int64_t)points.size(), indices, offsets, nullptr);
+}
+inline void findHalfNeighborList(cudaStream_t space, DeviceView<Point> const &points, float radius,
+                                 DeviceView<int> &offsets, DeviceView<int> &indices)
+{
+  abx_crs *crs = nullptr;
+  Details::check(abx_find_neighbor_list(space, reinterpret_cast<const float *>(points.data()),
+                                        (int64_t)points.size(), radius, 1, &crs));
+  Details::take(space, crs, (int64_t)points.size(), indices, offsets, nullptr);
+}
+} // namespace Experimental
+
+namespace Details
+{
+// expandHalfToFull (src/spatial/detail/ArborX_ExpandHalfToFull.hpp:23-69):
+// offsets and indices replaced by the full list.
+inline void expandHalfToFull(cudaStream_t space, DeviceView<int> &offsets, DeviceView<int> &indices)
+{
+  abx_crs *crs = nullptr;
+  const int64_t n = (int64_t)offsets.size() - 1;
+  check(abx_expand_half_to_full(space, n, offsets.data(), indices.data(), &crs));
+  DeviceView<int> new_offsets, new_indices;
+  take(space, crs, n, new_indices, new_offsets, nullptr);
+  offsets = new_offsets;
+  indices = new_indices;
+}
+} // namespace Details
 
 // ArborX::query(tree, space, predicates, indices, offsets[, policy])
 // (src/spatial/ArborX_CrsGraphWrapper.hpp:22-34).

@@ -255,6 +255,67 @@ static void knn_against_brute_force()
   CHECK(ok);
 }
 
+// BruteForce (src/spatial/ArborX_BruteForce.hpp) answers like the tree:
+// nearest exactly, intersects as multisets.
+static void brute_force_matches_tree()
+{
+  std::mt19937 gen(11);
+  std::uniform_real_distribution<float> u(0.f, 1.f);
+  std::vector<Point> pts(3000), qs(500);
+  for (auto &p : pts)
+    p = Point{{u(gen), u(gen), u(gen)}};
+  for (auto &q : qs)
+    q = Point{{u(gen), u(gen), u(gen)}};
+  DeviceView<Point> dp(pts), dq(qs);
+  BVH tree(nullptr, dp);
+  BruteForce brute(nullptr, dp);
+  CHECK(brute.size() == 3000);
+  DeviceView<int> ti, to, bi, bo;
+  tree.query(nullptr, nearest(dq, 7), ti, to);
+  brute.query(nullptr, nearest(dq, 7), bi, bo);
+  CHECK(ti.to_host() == bi.to_host() && to.to_host() == bo.to_host());
+  auto spheres = Experimental::make_intersects(qs, 0.05f);
+  tree.query(nullptr, spheres, ti, to);
+  brute.query(nullptr, spheres, bi, bo);
+  CHECK(same_crs({bo.to_host(), bi.to_host()}, to.to_host(), ti.to_host()));
+}
+
+// test/tstNeighborList.cpp:136-171 (rows as multisets).
+static void neighbor_lists()
+{
+  DeviceView<Point> pts(std::vector<Point>{{{0, 0, 0}}, {{1, 1, 1}}, {{2, 2, 2}}, {{3, 3, 3}}});
+  DeviceView<int> off, ind;
+  Experimental::findFullNeighborList(nullptr, pts, 2.f, off, ind);
+  CHECK(same_crs({off.to_host(), ind.to_host()}, {0, 1, 3, 5, 6}, {1, 0, 2, 1, 3, 2}));
+  Experimental::findHalfNeighborList(nullptr, pts, 4.f, off, ind);
+  Details::expandHalfToFull(nullptr, off, ind);
+  CHECK(same_crs({off.to_host(), ind.to_host()}, {0, 2, 5, 8, 10},
+                 {1, 2, 0, 2, 3, 0, 1, 3, 1, 2}));
+}
+
+// test/tstQueryTreeRay.cpp:62-171: rays through ten boxes on the diagonal.
+static void ordered_rays()
+{
+  std::vector<Box> boxes;
+  for (int i = 0; i < 10; ++i)
+    boxes.emplace_back(Point{{(float)i, (float)i, (float)i}},
+                       Point{{(float)i + 1, (float)i + 1, (float)i + 1}});
+  DeviceView<Box> db(boxes);
+  BVH tree(nullptr, db);
+  using Experimental::Ray;
+  DeviceView<Ray> rays(std::vector<Ray>{Ray{{{0, 0, 0}}, {{.1f, .1f, .1f}}},
+                                        Ray{{{10, 10, 10}}, {{-.1f, -.1f, -.1f}}}});
+  DeviceView<int> ind, off;
+  tree.query(nullptr, Experimental::make_ordered_intersects(rays), ind, off);
+  std::vector<int> want{0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 9, 8, 7, 6, 5, 4, 3, 2, 1, 0};
+  CHECK(ind.to_host() == want);
+  CHECK((off.to_host() == std::vector<int>{0, 10, 20}));
+  tree.query(nullptr, intersects(rays), ind, off);
+  CHECK((off.to_host() == std::vector<int>{0, 10, 20}));
+  tree.query(nullptr, Experimental::make_ordered_intersects(rays, 1), ind, off);
+  CHECK((ind.to_host() == std::vector<int>{0, 9}));
+}
+
 int main()
 {
   empty_tree();
@@ -266,6 +327,9 @@ int main()
   structured_grid();
   stack_capacity();
   knn_against_brute_force();
+  brute_force_matches_tree();
+  neighbor_lists();
+  ordered_rays();
   std::printf("%d checks, %d failures\n", g_checks, g_failures);
   return g_failures == 0 ? 0 : 1;
 }

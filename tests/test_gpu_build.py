@@ -178,7 +178,7 @@ def _hybrid_cases(n, seed):
     return [uniform, clustered, same_top, equal, mixed]
 
 
-@pytest.mark.parametrize("top", ["0", "3"])
+@pytest.mark.parametrize("top", ["0", "3", "4"])
 def test_sort_u64_hybrid_top_passes(ax, top):
     """The top-digit passes + run fix-up (+ long-run segmented sort) give the
     full stable sort on uniform, clustered, one-run and all-equal keys."""
