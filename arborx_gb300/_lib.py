@@ -40,7 +40,7 @@ class TraversalPolicyC(ctypes.Structure):
 
 
 class ServerConfigC(ctypes.Structure):
-    _fields_ = [("workers", ctypes.c_int32), ("reserved", ctypes.c_int32),
+    _fields_ = [("workers", ctypes.c_int32), ("l2_persist", ctypes.c_int32),
                 ("max_inflight_bytes", ctypes.c_int64), ("max_batch_queries", ctypes.c_int64)]
 
 

@@ -192,6 +192,13 @@ void dfree(void *p, cudaStream_t s)
     cudaFreeAsync(p, s);
 }
 
+// The child-pair nodes of a tree (the array every query reads most).
+void tree_node_memory(const abx_bvh *t, const void **ptr, size_t *bytes)
+{
+  *ptr = t ? t->tnodes : nullptr;
+  *bytes = t && t->tnodes ? (size_t)std::max<int64_t>(t->n - 1, 1) * sizeof(TNode) : 0;
+}
+
 } // namespace abx
 
 using namespace abx;

@@ -125,6 +125,9 @@ abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,
                           const uint32_t *d_hist, int top_passes = 0);
 
+// The child-pair node array of a tree (pointer and bytes).
+void tree_node_memory(const abx_bvh *t, const void **ptr, size_t *bytes);
+
 // Kernel attributes of the sort, set once per device by device_state().
 abx_status init_sort_kernels();
 

@@ -84,6 +84,10 @@ struct abx_server
   bool any_submit = false;
 
   std::vector<std::thread> workers;
+  // L2 persistence: the context limit before the server raised it
+  size_t persist_max = 0;
+  size_t persist_old = 0;
+  int max_window = 0;
 };
 
 namespace
@@ -225,6 +229,24 @@ abx_status run_batch(abx_server *srv, cudaStream_t s, WorkerBuffers &wb,
         st = cuda_fail(e, "k to device");
         break;
       }
+    }
+    if (srv->persist_max > 0)
+    {
+      // keep this tree's nodes in L2 against the streaming queries and results
+      const void *base = nullptr;
+      size_t bytes = 0;
+      abx::tree_node_memory(tree, &base, &bytes);
+      cudaStreamAttrValue attr = {};
+      attr.accessPolicyWindow.base_ptr = const_cast<void *>(base);
+      attr.accessPolicyWindow.num_bytes = std::min<size_t>(bytes, (size_t)srv->max_window);
+      attr.accessPolicyWindow.hitRatio =
+          attr.accessPolicyWindow.num_bytes
+              ? (float)std::min(1.0, (double)srv->persist_max /
+                                         (double)attr.accessPolicyWindow.num_bytes)
+              : 0.f;
+      attr.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+      attr.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+      cudaStreamSetAttribute(s, cudaStreamAttributeAccessPolicyWindow, &attr);
     }
     abx_traversal_policy policy{0, 1};
     if (kind == ABX_REQ_NEAREST)
@@ -387,6 +409,21 @@ abx_status abx_server_create(const abx_server_config *cfg, abx_server **out)
   srv->cfg = c;
   cudaGetDevice(&srv->device);
   abx::device_state();
+  if (c.l2_persist)
+  {
+    int max_persist = 0, max_window = 0;
+    cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, srv->device);
+    cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, srv->device);
+    size_t old = 0;
+    if (max_persist > 0 && max_window > 0 &&
+        cudaDeviceGetLimit(&old, cudaLimitPersistingL2CacheSize) == cudaSuccess &&
+        cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, (size_t)max_persist) == cudaSuccess)
+    {
+      srv->persist_old = old;
+      srv->persist_max = (size_t)max_persist;
+      srv->max_window = max_window;
+    }
+  }
   try
   {
     for (int w = 0; w < c.workers; ++w)
@@ -420,6 +457,12 @@ abx_status abx_server_destroy(abx_server *srv)
   srv->cv_mem.notify_all();
   for (auto &t : srv->workers)
     t.join();
+  if (srv->persist_max > 0)
+  {
+    // give the persisting lines back and restore the context's limit
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, srv->persist_old);
+  }
   delete srv;
   return ABX_SUCCESS;
 }

@@ -18,10 +18,11 @@ from ._lib import REQ_INTERSECTS, REQ_NEAREST, RequestC, ServerConfigC, ServerSt
 
 
 class Server:
-    def __init__(self, workers=4, max_inflight_bytes=8 << 30, max_batch_queries=1 << 20):
+    def __init__(self, workers=4, max_inflight_bytes=8 << 30, max_batch_queries=1 << 20,
+                 l2_persist=False):
         L = _lib.load()
         self._h = ctypes.c_void_p()
-        cfg = ServerConfigC(workers, 0, max_inflight_bytes, max_batch_queries)
+        cfg = ServerConfigC(workers, 1 if l2_persist else 0, max_inflight_bytes, max_batch_queries)
         check(L.abx_server_create(ctypes.byref(cfg), ctypes.byref(self._h)))
         self._trees = []
         self._meta = {}
