@@ -436,20 +436,24 @@ struct SortedLeaf<1>
 };
 
 // Segment containing global position i of a batch of trees: the largest s
-// with off[s] <= i (empty trees share offsets with their successor and are
-// skipped).
-__device__ __forceinline__ int find_segment(const int64_t *__restrict__ off, int nseg, int64_t i)
+// in [lo, hi] with off[s] <= i (empty trees share offsets with their
+// successor and are skipped).  The caller knows i lies in segments lo..hi.
+__device__ __forceinline__ int find_segment_in(const int64_t *off, int lo, int hi, int64_t i)
 {
-  int lo = 0, hi = nseg - 1;
   while (lo < hi)
   {
     const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(off + mid) <= i)
+    if (off[mid] <= i)
       lo = mid;
     else
       hi = mid - 1;
   }
   return lo;
+}
+
+__device__ __forceinline__ int find_segment(const int64_t *__restrict__ off, int nseg, int64_t i)
+{
+  return find_segment_in(off, 0, nseg - 1, i);
 }
 
 // ---------------------------------------------------------------------------

@@ -37,14 +37,15 @@ __device__ __forceinline__ long long seg_delta(const uint64_t *__restrict__ code
   return (long long)(x + add - 1ull);
 }
 
-// delta at global position j, whatever tree j belongs to.
+// delta at global position j, whatever tree j belongs to (its tree among
+// segments s_lo..s_hi).
 __device__ __forceinline__ long long pos_delta(const uint64_t *__restrict__ codes,
-                                               const int64_t *__restrict__ off, int nseg,
-                                               int64_t total, int j)
+                                               const int64_t *__restrict__ off, int s_lo,
+                                               int s_hi, int64_t total, int j)
 {
   if (j < 0 || (int64_t)j >= total - 1)
     return LLONG_MAX;
-  const int s = find_segment(off, nseg, j);
+  const int s = find_segment_in(off, s_lo, s_hi, j);
   return seg_delta(codes, j, (int)__ldg(off + s), (int)__ldg(off + s + 1) - 1);
 }
 
@@ -256,21 +257,28 @@ __global__ void __launch_bounds__(kHierBlock)
   __shared__ int3 s_items[2][kHierBlock];       // (range_left, range_right, node or -1)
   __shared__ int s_count[2];
 
+  __shared__ int s_seg[2]; // the trees of positions b0 - 1 .. b1 + 1
   const int b0 = blockIdx.x * kHierBlock;
   const int b1 = (int)min((int64_t)b0 + kHierBlock - 1, total - 1);
   const int nb = b1 - b0 + 1;
   const int tid = threadIdx.x;
   const int lane = tid & 31;
+  if (tid < 2)
+    s_seg[tid] = nseg > 1 ? find_segment(off, nseg,
+                                         tid == 0 ? max(b0 - 1, 0) : min((int64_t)b1 + 1, total - 1))
+                          : 0;
+  __syncthreads();
+  const int seg_lo = s_seg[0], seg_hi = s_seg[1];
 
   for (int k = tid; k <= nb; k += blockDim.x)
-    s_delta[k] = pos_delta(codes, off, nseg, total, b0 - 1 + k);
+    s_delta[k] = pos_delta(codes, off, seg_lo, seg_hi, total, b0 - 1 + k);
   s_flag[tid] = -1;
   if (tid < 2)
     s_count[tid] = 0;
   const int i = b0 + tid;
   if (i <= b1)
   {
-    const int s = nseg > 1 ? find_segment(off, nseg, i) : 0;
+    const int s = find_segment_in(off, seg_lo, seg_hi, i);
     const int lo = (int)__ldg(off + s);
     const int hi = (int)__ldg(off + s + 1) - 1;
     const int original = (int)__ldg(perm + i);
@@ -348,7 +356,7 @@ __global__ void __launch_bounds__(kHierBlock)
       st.range_right = R;
       st.cur_node = node;
       st.value = node < 0 ? s_value[L - b0] : 0;
-      const int s = nseg > 1 ? find_segment(off, nseg, L) : 0;
+      const int s = find_segment_in(off, seg_lo, seg_hi, L);
       st.lo = (int)__ldg(off + s);
       st.hi = (int)__ldg(off + s + 1) - 1;
       st.pad[0] = st.pad[1] = 0;
@@ -646,13 +654,38 @@ __global__ void __launch_bounds__(256)
       atomicAdd(&hist[k], sh[k]);
 }
 
-// keys[i] = tree of the value at sorted position i.
+// keys[i] = tree of the value at sorted position i (its original index is
+// random, so the search runs over a shared-memory copy of the offsets when
+// they fit).
+constexpr int kSmemOffsets = 6144;
+
 __global__ void k_tree_keys(const uint32_t *__restrict__ perm, const int64_t *__restrict__ off,
                             int nseg, int64_t total, uint32_t *__restrict__ keys)
 {
+  __shared__ int64_t s_off[kSmemOffsets];
+  const bool staged = nseg + 1 <= kSmemOffsets;
+  if (staged)
+    for (int k = threadIdx.x; k <= nseg; k += blockDim.x)
+      s_off[k] = off[k];
+  __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < total)
-    keys[i] = (uint32_t)find_segment(off, nseg, perm[i]);
+    keys[i] = (uint32_t)(staged ? find_segment_in(s_off, 0, nseg - 1, perm[i])
+                                : find_segment(off, nseg, perm[i]));
+}
+
+// The trees of a CTA's consecutive positions [first, first + blockDim.x):
+// thread 0 and 1 find the two ends once.
+__device__ __forceinline__ void block_segments(const int64_t *__restrict__ off, int nseg,
+                                               int64_t first, int64_t total, int *s_seg)
+{
+  if (threadIdx.x < 2)
+  {
+    const int64_t p =
+        threadIdx.x == 0 ? first : min(first + (int64_t)blockDim.x - 1, total - 1);
+    s_seg[threadIdx.x] = find_segment(off, nseg, p);
+  }
+  __syncthreads();
 }
 
 // Morton64 code of the value at every sorted position (after the regroup by
@@ -662,10 +695,13 @@ __global__ void k_forest_codes(const float *__restrict__ g, const uint32_t *__re
                                const int64_t *__restrict__ off, int nseg, int64_t total,
                                const float *__restrict__ bounds, uint64_t *__restrict__ codes)
 {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ int s_seg[2];
+  const int64_t first = (int64_t)blockIdx.x * blockDim.x;
+  block_segments(off, nseg, first, total, s_seg);
+  const int64_t i = first + threadIdx.x;
   if (i >= total)
     return;
-  const int s = find_segment(off, nseg, i);
+  const int s = find_segment_in(off, s_seg[0], s_seg[1], i);
   float sc[6];
 #pragma unroll
   for (int d = 0; d < 6; ++d)
@@ -677,22 +713,34 @@ __global__ void k_forest_codes(const float *__restrict__ g, const uint32_t *__re
 
 // Predicate ordering key of a forest query: its tree above the Morton32 code
 // of its centroid in that tree's box (ArborX_LinearBVH.hpp:287-306 per tree).
-template <int KIND>
+// A 32-bit key keeps the top 32 - tree_bits bits of the 30-bit code (the
+// order only serves coherence); otherwise tree << 32 | code.
+template <int KIND, class Key>
 __global__ void k_forest_query_keys(const float *__restrict__ preds,
-                                    const int64_t *__restrict__ qoff, int nseg, int64_t nq,
-                                    const float *__restrict__ bounds, uint64_t *__restrict__ keys)
+                                    const int64_t *__restrict__ qoff, int nseg, int tree_bits,
+                                    int64_t nq, const float *__restrict__ bounds,
+                                    Key *__restrict__ keys)
 {
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  __shared__ int s_seg[2];
+  const int64_t first = (int64_t)blockIdx.x * blockDim.x;
+  block_segments(qoff, nseg, first, nq, s_seg);
+  const int64_t q = first + threadIdx.x;
   if (q >= nq)
     return;
-  const int s = find_segment(qoff, nseg, q);
+  const int s = find_segment_in(qoff, s_seg[0], s_seg[1], q);
   const float *sc = bounds + 6 * s;
   float x, y, z;
   load_centroid<KIND>(preds, q, x, y, z);
   const uint32_t c = morton32_unit(translate_scale(x, __ldg(sc), __ldg(sc + 3)),
                                    translate_scale(y, __ldg(sc + 1), __ldg(sc + 4)),
                                    translate_scale(z, __ldg(sc + 2), __ldg(sc + 5)));
-  keys[q] = ((uint64_t)s << 32) | c;
+  if (sizeof(Key) == 8)
+    keys[q] = (Key)(((uint64_t)s << 32) | c);
+  else
+  {
+    const int shift = tree_bits > 2 ? tree_bits - 2 : 0;
+    keys[q] = (Key)((tree_bits ? ((uint32_t)s << (32 - tree_bits)) : 0u) | (c >> shift));
+  }
 }
 
 __global__ void k_one_segment(int64_t *off, int64_t n)
@@ -888,19 +936,36 @@ abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const floa
 {
   if (nq < 1)
     return ABX_SUCCESS;
-  Scratch<uint64_t> keys;
-  ABX_CUDA_TRY(keys.alloc(nq, s));
-  const unsigned blocks = (unsigned)((nq + 255) / 256);
-  if (pred_kind == ABX_POINT)
-    k_forest_query_keys<0><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, nq, d_bounds, keys.ptr);
-  else if (pred_kind == ABX_BOX)
-    k_forest_query_keys<1><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, nq, d_bounds, keys.ptr);
-  else
-    k_forest_query_keys<2><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, nq, d_bounds, keys.ptr);
-  ABX_CUDA_TRY(cudaGetLastError());
   int tree_bits = 0;
   while ((1ll << tree_bits) < nseg)
     ++tree_bits;
+  const unsigned blocks = (unsigned)((nq + 255) / 256);
+#define ABX_QKEYS(KEY)                                                                        \
+  do                                                                                          \
+  {                                                                                           \
+    if (pred_kind == ABX_POINT)                                                               \
+      k_forest_query_keys<0, KEY><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, tree_bits, nq, \
+                                                        d_bounds, keys.ptr);                  \
+    else if (pred_kind == ABX_BOX)                                                            \
+      k_forest_query_keys<1, KEY><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, tree_bits, nq, \
+                                                        d_bounds, keys.ptr);                  \
+    else                                                                                      \
+      k_forest_query_keys<2, KEY><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, tree_bits, nq, \
+                                                        d_bounds, keys.ptr);                  \
+    ABX_CUDA_TRY(cudaGetLastError());                                                         \
+  } while (0)
+  if (tree_bits <= 16)
+  {
+    Scratch<uint32_t> keys;
+    ABX_CUDA_TRY(keys.alloc(nq, s));
+    ABX_QKEYS(uint32_t);
+    // big trees hold many queries per top-digit cell: the plain LSD sort
+    return radix_sort_u32(s, keys.ptr, d_perm, nullptr, nq, 4, nullptr, 0);
+  }
+  Scratch<uint64_t> keys;
+  ABX_CUDA_TRY(keys.alloc(nq, s));
+  ABX_QKEYS(uint64_t);
+#undef ABX_QKEYS
   return radix_sort_u64(s, keys.ptr, d_perm, nullptr, nq, (32 + tree_bits + 7) / 8, nullptr);
 }
 

@@ -363,12 +363,12 @@ __global__ void __launch_bounds__(kQueryThreads)
     atomicOr(overflow, 1u);
 }
 
+// One thread per query: its first min(count, buffer) results from the
+// per-query buffer to the CRS (rows of a warp are adjacent in both arrays).
 __global__ void k_compact(const int32_t *__restrict__ tmp, int64_t nq, int32_t buffer,
                           const int32_t *__restrict__ offsets, int32_t *__restrict__ out)
 {
-  // one warp per query
-  const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nq)
     return;
   const int32_t o = offsets[q];
@@ -376,7 +376,7 @@ __global__ void k_compact(const int32_t *__restrict__ tmp, int64_t nq, int32_t b
   // pass rewrites all of them
   const int32_t c = min(offsets[q + 1] - o, buffer);
   const int32_t *src = tmp + q * (int64_t)buffer;
-  for (int j = lane; j < c; j += 32)
+  for (int32_t j = 0; j < c; ++j)
     out[o + j] = src[j];
 }
 
@@ -1316,7 +1316,7 @@ abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int3
 {
   if (nq <= 0)
     return ABX_SUCCESS;
-  const unsigned blocks = (unsigned)((nq * 32 + 255) / 256);
+  const unsigned blocks = (unsigned)((nq + 255) / 256);
   StageScope scope(s, "compact", 1);
   k_compact<<<blocks, 256, 0, s>>>(d_tmp, nq, buffer, d_offsets, d_out);
   ABX_CUDA_TRY(cudaGetLastError());

@@ -62,6 +62,8 @@ def parse():
                     help="skip the batched-vs-plain measurement in the headline line")
     ap.add_argument("--dist", default="uniform", choices=["uniform", "clustered"],
                     help="--case build/nearest/radius: point distribution")
+    ap.add_argument("--no-plain", action="store_true",
+                    help="--case forest: time the batched arm only")
     ap.add_argument("--serve-requests", type=int, default=2000)
     ap.add_argument("--l2-persist", action="store_true",
                     help="--case serve: L2-persisting window on the queried tree's nodes")
@@ -635,13 +637,33 @@ def measure_forest(clouds, warmup=2, steps=3, plain_steps=1):
         torch.cuda.synchronize()
         return (time.perf_counter() - t0) / n, r
 
+    import ctypes
+
+    from arborx_gb300 import _lib
+
+    L = _lib.load()
     for _ in range(warmup):
         batched()
+    L.abx_profiling_reset()
+    L.abx_profiling_enable(1)
     tb, (bi, bo) = timed(batched, steps)
-    plain()
-    tp, per = timed(plain, plain_steps)
+    L.abx_profiling_enable(0)
+    stages = {}
+    for name in ("bounds", "morton64", "sort64", "sort32", "hierarchy", "spatial", "scan"):
+        t = ctypes.c_double(0)
+        c = ctypes.c_int64(0)
+        L.abx_profiling_stage(name.encode(), ctypes.byref(t), ctypes.byref(c))
+        if c.value:
+            stages[name] = t.value / steps
+    L.abx_profiling_reset()
     bo_h = bo.cpu().numpy()
     bi_h = bi.cpu().numpy()
+    if plain_steps <= 0:  # batched arm alone (profiling captures)
+        total = int(off[-1])
+        return {"workload": "%d clouds, %d points" % (ntrees, total), "batched_ms": tb * 1e3,
+                "batched_stages_ms": stages, "results": int(bo_h[-1])}
+    plain()
+    tp, per = timed(plain, plain_steps)
     same = True
     for t, (i, o) in enumerate(per):
         seg = bo_h[off[t]:off[t + 1] + 1]
@@ -655,6 +677,7 @@ def measure_forest(clouds, warmup=2, steps=3, plain_steps=1):
         % (ntrees, total),
         "results": int(bo_h[-1]),
         "batched_ms": tb * 1e3, "plain_ms": tp * 1e3, "speedup": tp / tb,
+        "batched_stages_ms": stages,
         "batched_points_per_s": total / tb, "plain_points_per_s": total / tp,
         "bit_exact": same,
     }
@@ -664,10 +687,11 @@ def run_forest(args):
     from arborx_gb300 import build as libbuild
 
     libbuild.build()
-    res = measure_forest(args.clouds, args.warmup, args.steps, max(1, min(args.steps, 3)))
+    res = measure_forest(args.clouds, args.warmup, args.steps,
+                         0 if args.no_plain else max(1, min(args.steps, 3)))
     res["case"] = "forest"
     print(json.dumps(res), flush=True)
-    if not res["bit_exact"]:
+    if not res.get("bit_exact", True):
         sys.exit(1)
 
 
