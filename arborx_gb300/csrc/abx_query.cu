@@ -363,21 +363,47 @@ __global__ void __launch_bounds__(kQueryThreads)
     atomicOr(overflow, 1u);
 }
 
-// One thread per query: its first min(count, buffer) results from the
-// per-query buffer to the CRS (rows of a warp are adjacent in both arrays).
+// Compaction of per-query buffers into the CRS.  A warp owns 32 consecutive
+// queries and copies their contiguous output range: each lane takes output
+// positions with stride 32, finds its query by a binary search over the 33
+// offsets held in the lanes' registers, and reads entry (position - offset)
+// of that query's buffer.  Stores are coalesced for any row length.  An
+// overflowed query keeps its first `buffer` results here; the fill pass
+// rewrites all of them.
 __global__ void k_compact(const int32_t *__restrict__ tmp, int64_t nq, int32_t buffer,
                           const int32_t *__restrict__ offsets, int32_t *__restrict__ out)
 {
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= nq)
+  const int64_t q0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5 << 5;
+  const int lane = threadIdx.x & 31;
+  if (q0 >= nq)
     return;
-  const int32_t o = offsets[q];
-  // an overflowed query keeps its first `buffer` results here; the fill
-  // pass rewrites all of them
-  const int32_t c = min(offsets[q + 1] - o, buffer);
-  const int32_t *src = tmp + q * (int64_t)buffer;
-  for (int32_t j = 0; j < c; ++j)
-    out[o + j] = src[j];
+  const int m = (int)min((int64_t)32, nq - q0); // queries of this warp
+  // lane l holds offsets[q0 + l] for l < m
+  const int32_t my_off = lane < m ? offsets[q0 + lane] : INT32_MAX;
+  const int32_t begin = __shfl_sync(0xffffffffu, my_off, 0);
+  const int32_t end = offsets[q0 + m];
+  for (int32_t base = begin; base < end; base += 32) // warp-uniform trips
+  {
+    const int32_t j = base + lane;
+    // the largest r < m with offsets[q0 + r] <= j
+    int lo = 0, hi = m - 1;
+#pragma unroll
+    for (int step = 0; step < 5; ++step)
+    {
+      const int mid = (lo + hi + 1) >> 1;
+      const int32_t om = __shfl_sync(0xffffffffu, my_off, mid);
+      if (lo < hi)
+      {
+        if (om <= j)
+          lo = mid;
+        else
+          hi = mid - 1;
+      }
+    }
+    const int32_t e = j - __shfl_sync(0xffffffffu, my_off, lo);
+    if (j < end && e < buffer)
+      out[j] = tmp[(q0 + lo) * (int64_t)buffer + e];
+  }
 }
 
 // Queries whose result count exceeds the buffer: flag[q] = 1.
@@ -1316,7 +1342,7 @@ abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int3
 {
   if (nq <= 0)
     return ABX_SUCCESS;
-  const unsigned blocks = (unsigned)((nq + 255) / 256);
+  const unsigned blocks = (unsigned)((nq + 255) / 256); // a warp per 32 queries
   StageScope scope(s, "compact", 1);
   k_compact<<<blocks, 256, 0, s>>>(d_tmp, nq, buffer, d_offsets, d_out);
   ABX_CUDA_TRY(cudaGetLastError());
