@@ -192,6 +192,19 @@ void dfree(void *p, cudaStream_t s)
     cudaFreeAsync(p, s);
 }
 
+// Top passes of the code sort from the Morton kernel's digit histograms
+// (one small read back; plain sort choice for clustered codes).
+int top_passes_from_hist(cudaStream_t s, const uint32_t *d_hist, int64_t n)
+{
+  if (hybrid_top_passes(n, 8) <= 0)
+    return 0;
+  uint32_t h[8 * 256];
+  if (cudaMemcpyAsync(h, d_hist, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return hybrid_top_passes(n, 8);
+  return choose_top_passes(h, n, 8);
+}
+
 // The child-pair nodes of a tree (the array every query reads most).
 void tree_node_memory(const abx_bvh *t, const void **ptr, size_t *bytes)
 {
@@ -290,7 +303,7 @@ abx_status build_tree(abx_bvh *t, const float *d_values)
     ABX_TRY(scene_bounds(s, t->kind, d_values, n, t->d_bounds));
     ABX_TRY(morton64_codes(s, t->kind, d_values, n, t->d_bounds, codes.ptr, hist.ptr));
     ABX_TRY(radix_sort_u64(s, codes.ptr, perm.ptr, nullptr, n, 8, hist.ptr,
-                           hybrid_top_passes(n, 8)));
+                           top_passes_from_hist(s, hist.ptr, n)));
     ABX_TRY(generate_hierarchy(s, t->kind, d_values, n, perm.ptr, codes.ptr, nullptr, nullptr,
                                t->tnodes, t->sorted));
   }

@@ -138,6 +138,14 @@ bool stream_capturing(cudaStream_t s);
 // (0 = plain LSD).
 int hybrid_top_passes(int64_t n, int num_passes);
 
+// Top passes of a Morton64 code sort from the device digit histograms
+// (reads them back: synchronises s).
+int top_passes_from_hist(cudaStream_t s, const uint32_t *d_hist, int64_t n);
+
+// Top passes chosen from the digit histograms (host copy, num_passes x 256)
+// of the keys: 3 or 4 when runs of equal top digits stay short, else 0.
+int choose_top_passes(const uint32_t *h_hist, int64_t n, int num_passes);
+
 // Exclusive scan of n int32 into n + 1 outputs; *d_total_out (optional,
 // device int64) receives the 64-bit total.  Raises ABX_DEVERR_BAD_INPUT when
 // the total does not fit in int32.

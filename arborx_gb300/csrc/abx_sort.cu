@@ -767,6 +767,31 @@ abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
                                    top_passes);
 }
 
+int choose_top_passes(const uint32_t *h_hist, int64_t n, int num_passes)
+{
+  const int cap = hybrid_top_passes(n, num_passes);
+  if (cap <= 0 || !h_hist)
+    return cap;
+  // expected keys sharing a key's top-digit cell, digits taken independent:
+  // n * prod_d sum_b p_d(b)^2 (about 1.2 for 1e7 uniform Morton codes with 3
+  // digits); clustered keys make it large
+  double collide = 1.0;
+  for (int t = 1; t <= 4 && t < num_passes; ++t)
+  {
+    const uint32_t *h = h_hist + (size_t)(num_passes - t) * kBins;
+    double sq = 0.0;
+    for (int b = 0; b < kBins; ++b)
+    {
+      const double p = (double)h[b] / (double)n;
+      sq += p * p;
+    }
+    collide *= sq;
+    if (t >= 3 && (double)n * collide <= 4.0)
+      return t;
+  }
+  return 0;
+}
+
 int hybrid_top_passes(int64_t n, int num_passes)
 {
   // 3 top digits (24 bits) spread up to ~2^24 keys into short runs, 4 digits
