@@ -12,7 +12,7 @@ All compute runs in libarborx_gb300.so; tensors are passed as raw device
 pointers and results are zero-copy views of the library's own buffers.
 """
 
-from ._lib import BOX, POINT, RAY, SPHERE, AbxError, SearchException  # noqa: F401
+from ._lib import BOX, KDOP6, KDOP14, KDOP18, KDOP26, POINT, RAY, SPHERE, AbxError, SearchException  # noqa: F401
 from .serve import Server  # noqa: F401
 from .bvh import (  # noqa: F401
     BoundingVolumeHierarchy,
@@ -28,6 +28,7 @@ from .bvh import (  # noqa: F401
     find_half_neighbor_list,
     generate_hierarchy,
     intersects,
+    kdop_from,
     make_intersects,
     make_nearest,
     morton32,

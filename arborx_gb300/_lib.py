@@ -22,6 +22,9 @@ ERROR_TIMEOUT = 7
 
 # abx_geometry
 POINT, BOX, SPHERE, RAY = 0, 1, 2, 3
+# KDOP<3, k> geometry kinds and their number of directions (k / 2)
+KDOP6, KDOP14, KDOP18, KDOP26 = 4, 5, 6, 7
+KDOP_NDIR = {KDOP6: 3, KDOP14: 7, KDOP18: 9, KDOP26: 13}
 
 # Every function the header declares: name -> (restype, argtypes)
 _P = ctypes.c_void_p
@@ -75,6 +78,10 @@ SIGNATURES = {
     "abx_profiling_reset": (_STATUS, []),
     "abx_bvh_create": (_STATUS, [_P, ctypes.c_int, _P, _I64, ctypes.POINTER(_P)]),
     "abx_bvh_create_strided": (_STATUS, [_P, ctypes.c_int, ValuesC, _I64, ctypes.POINTER(_P)]),
+    "abx_kdop_from_geometry": (_STATUS, [_P, ctypes.c_int, _P, _I64, ctypes.c_int, _P]),
+    "abx_bvh_kdop_bounds": (_STATUS, [_P, _P]),
+    "abx_bvh_save": (_STATUS, [_P, ctypes.c_char_p]),
+    "abx_bvh_load": (_STATUS, [_P, ctypes.c_char_p, ctypes.POINTER(_P)]),
     "abx_bvh_destroy": (_STATUS, [_P]),
     "abx_bvh_size": (_I64, [_P]),
     "abx_bvh_bounds": (_STATUS, [_P, _P]),

@@ -30,7 +30,7 @@ NVCC_FLAGS = ARCH + [
 
 SOURCES = [
     "abx_capi.cu", "abx_build.cu", "abx_hierarchy.cu", "abx_sort.cu", "abx_query.cu", "abx_serve.cu",
-    "abx_neighbors.cu", "abx_rays.cu",
+    "abx_neighbors.cu", "abx_rays.cu", "abx_kdop.cu",
 ]
 
 

@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from ._lib import BOX, POINT, RAY, SPHERE, TraversalPolicyC, check
+from ._lib import BOX, KDOP6, KDOP14, KDOP18, KDOP26, KDOP_NDIR, POINT, RAY, SPHERE, TraversalPolicyC, check
 
 
 def version():
@@ -100,13 +100,30 @@ class TraversalPolicy:
         return TraversalPolicyC(self._buffer_size, 1 if self._sort_predicates else 0)
 
 
+def _columns(kind):
+    """Floats per value of a geometry kind."""
+    if kind in KDOP_NDIR:
+        return 2 * KDOP_NDIR[kind]
+    return {POINT: 3, BOX: 6, SPHERE: 4, RAY: 6}[kind]
+
+
+def _kind_of(cols, what):
+    """Geometry kind of a value width (6 columns: a box; KDOP<3, 6> needs an
+    explicit kind)."""
+    kind = {3: POINT, 4: SPHERE, 6: BOX, 14: KDOP14, 18: KDOP18, 26: KDOP26}.get(cols)
+    if kind is None:
+        raise ValueError("%s: no geometry has %d columns" % (what, cols))
+    return kind
+
+
 class Intersects:
-    """Batch of intersects(geometry) predicates: spheres [nq,4] (cx cy cz r)
-    or boxes [nq,6] (min xyz, max xyz)."""
+    """Batch of intersects(geometry) predicates: spheres [nq,4] (cx cy cz r),
+    boxes [nq,6] (min xyz, max xyz), rays [nq,6] or KDOP<3, k> [nq, k]
+    (min of the k/2 directions, then max)."""
 
     def __init__(self, geometry, kind):
         self.kind = kind
-        self.data = _as_rows(geometry, 4 if kind == SPHERE else 6, "intersects geometry")
+        self.data = _as_rows(geometry, _columns(kind), "intersects geometry")
 
     def __len__(self):
         return self.data.shape[0]
@@ -151,13 +168,29 @@ class Nearest:
 
 
 def intersects(geometry, kind=None):
+    """intersects(Sphere | Box | KDOP) predicates; the kind follows the number
+    of columns (4 sphere, 6 box, 14 / 18 / 26 KDOP) unless given."""
     g = geometry
     if kind is None:
-        cols = g.shape[-1]
-        kind = {4: SPHERE, 6: BOX}.get(cols)
-        if kind is None:
-            raise ValueError("intersects: geometry must have 4 (sphere) or 6 (box) columns")
+        kind = _kind_of(g.shape[-1], "intersects")
+        if kind == POINT:
+            raise ValueError("intersects: points are predicates as degenerate boxes [p, p]")
     return Intersects(g, kind)
+
+
+def kdop_from(geometry, k, kind=None, space=None):
+    """KDOP<3, k> (k = 6, 14, 18, 26) of every point [n, 3] or box [n, 6]:
+    KDOP{} expanded by the geometry (abx_kdop_from_geometry).  Returns a
+    float32 CUDA tensor [n, k]."""
+    kk = {6: KDOP6, 14: KDOP14, 18: KDOP18, 26: KDOP26}[int(k)]
+    if kind is None:
+        kind = {3: POINT, 6: BOX}.get(geometry.shape[-1])
+        if kind is None:
+            raise ValueError("kdop_from: points [n, 3] or boxes [n, 6]")
+    g = _as_rows(geometry, _columns(kind), "geometry")
+    out = torch.empty((g.shape[0], int(k)), dtype=torch.float32, device=g.device)
+    check(_lib.load().abx_kdop_from_geometry(_stream(space), kind, _ptr(g), g.shape[0], kk, _ptr(out)))
+    return out
 
 
 def nearest(points, k=1):
@@ -177,8 +210,10 @@ def make_nearest(points, k):
 
 
 class BoundingVolumeHierarchy:
-    """Tree over points [n,3] or boxes [n,6]; the value of each leaf is its
-    row index (ArborX's benchmark form BVH<MemorySpace, int, ...>)."""
+    """Tree over points [n,3], boxes [n,6] or KDOP<3, k> [n, k] (nodes then
+    bounded by KDOPs too: BVH<MemorySpace, Value, IndexableGetter, KDOP>); the
+    value of each leaf is its row index (ArborX's benchmark form
+    BVH<MemorySpace, int, ...>)."""
 
     def __init__(self, values=None, space=None, kind=None):
         L = _lib.load()
@@ -187,12 +222,12 @@ class BoundingVolumeHierarchy:
             values = torch.empty((0, 3), dtype=torch.float32, device="cuda")
             kind = POINT
         if kind is None:
-            kind = {3: POINT, 6: BOX}.get(values.shape[-1])
-            if kind is None:
-                raise ValueError("values must have 3 (point) or 6 (box) columns")
+            kind = _kind_of(values.shape[-1], "values")
+            if kind not in (POINT, BOX) and kind not in KDOP_NDIR:
+                raise ValueError("values must be points, boxes or KDOPs")
         self.kind = kind
         self._stream = _stream(space)
-        cols = 3 if kind == POINT else 6
+        cols = _columns(kind)
         if (isinstance(values, torch.Tensor) and values.is_cuda and values.dtype == torch.float32
                 and values.dim() == 2 and values.shape[1] == cols and not values.is_contiguous()):
             # any layout (access traits): read through the tensor's strides
@@ -238,6 +273,27 @@ class BoundingVolumeHierarchy:
 
     def query(self, predicates, policy=None, space=None, with_distances=False):
         return query(self, predicates, policy, space=space, with_distances=with_distances)
+
+    def kdop_bounds(self):
+        """The KDOP of the whole tree (KDOP trees); waits for the build."""
+        out = (ctypes.c_float * (2 * KDOP_NDIR[self.kind]))()
+        check(_lib.load().abx_bvh_kdop_bounds(self._h, out))
+        return tuple(out)
+
+    def save(self, path):
+        """Write the tree to a file (abx_bvh_save)."""
+        check(_lib.load().abx_bvh_save(self._h, str(path).encode()))
+
+    @classmethod
+    def load(cls, path, space=None):
+        """A tree read back from a file written by save() (abx_bvh_load)."""
+        t = cls.__new__(cls)
+        t._h = ctypes.c_void_p()
+        t._stream = _stream(space)
+        check(_lib.load().abx_bvh_load(t._stream, str(path).encode(), ctypes.byref(t._h)))
+        t.kind = int(_lib.load().abx_bvh_geometry(t._h))
+        t._values = None
+        return t
 
 
 BVH = BoundingVolumeHierarchy

@@ -316,6 +316,16 @@ abx_status morton32_codes(cudaStream_t s, abx_geometry kind, const float *d_g, i
     k_morton32<2><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
   else if (kind == ABX_RAY)
     k_morton32<3><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
+  else if (kind == ABX_KDOP6)
+    k_morton32<4><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
+  else if (kind == ABX_KDOP14)
+    k_morton32<5><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
+  else if (kind == ABX_KDOP18)
+    k_morton32<6><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
+  else if (kind == ABX_KDOP26)
+    k_morton32<7><<<blocks, 256, 0, s>>>(d_g, n, d_scene, d_codes, d_hist);
+  else
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "predicate kind");
   ABX_CUDA_TRY(cudaGetLastError());
   return ABX_SUCCESS;
 }

@@ -86,6 +86,11 @@ struct TreeView
   const float *d_bounds; // 6 floats, the tree bounds
   const float4 *sorted;  // leaf geometry in Morton order (SortedLeaf<kind>)
   abx_geometry kind;     // ABX_POINT or ABX_BOX leaves
+  // KDOP-bounded trees (abx_kdop.cu): directions (0: box-bounded), node slot
+  // and leaf KDOP records
+  int ndir = 0;
+  const float *knodes = nullptr;
+  const float *kleaves = nullptr;
 };
 
 // Trees of a batch seen by a query launch: tree s owns the sorted positions
@@ -116,6 +121,26 @@ enum SpatialMode
   kFill = 1,   // out[offsets[q] + j] = j-th hit
   kBuffered = 2 // out[q * buffer + j] for j < buffer, counts[q] = hits
 };
+
+// KDOPs (abx_kdop.cu).  kdop_from_geometry: expand(KDOP{}, point or box)
+// for n points or boxes into the host KDOP format.  kdop_axis_boxes: the axis
+// box of every KDOP.  kdop_records: the node slot and leaf records of a KDOP
+// tree of n >= 1 values over its box topology (d_knodes: 2 max(n - 1, 1) + 1
+// records, d_kleaves: n records of kdop_pad(ndir) floats).
+abx_status kdop_from_geometry(cudaStream_t s, abx_geometry src_kind, const float *d_src, int64_t n,
+                              abx_geometry kdop_kind, float *d_out);
+abx_status kdop_axis_boxes(cudaStream_t s, abx_geometry kdop_kind, const float *d_kdops, int64_t n,
+                           float *d_boxes);
+abx_status kdop_records(cudaStream_t s, abx_geometry kdop_kind, const TNode *d_tnodes,
+                        const float4 *d_sorted, int64_t n, const float *d_kdops, float4 *d_knodes,
+                        float4 *d_kleaves);
+// Spatial launches that involve KDOPs: KDOP predicates on any tree or brute
+// force, and box or KDOP predicates on KDOP trees.
+abx_status launch_spatial_kdop(cudaStream_t s, TreeView const &t, ForestView const &f,
+                               abx_geometry pred_kind, const float *d_preds, int64_t nq,
+                               const uint32_t *d_perm, SpatialMode mode, int32_t *d_counts,
+                               const int32_t *d_offsets, int32_t *d_out, int32_t buffer,
+                               unsigned *d_overflow);
 
 abx_status launch_spatial(cudaStream_t s, TreeView const &t, ForestView const *f,
                           abx_geometry pred_kind, const float *d_preds, int64_t nq,

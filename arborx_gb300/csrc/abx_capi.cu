@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <atomic>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
@@ -14,6 +15,7 @@
 #include <vector>
 
 #include "abx_build.h"
+#include "abx_kdop.cuh"
 
 // ---------------------------------------------------------------------------
 // Opaque objects
@@ -35,6 +37,13 @@ struct abx_bvh
   int32_t ntrees = 1;
   std::vector<int64_t> h_off;
   int64_t *d_off = nullptr;
+  // a tree over KDOP values (abx_kdop.cu): `kind` is ABX_BOX (the values'
+  // axis boxes give the topology and `sorted`), kdop_kind the values' kind,
+  // ndir its number of directions, knodes / kleaves the KDOP records
+  int ndir = 0;
+  abx_geometry kdop_kind = ABX_BOX;
+  float4 *knodes = nullptr;
+  float4 *kleaves = nullptr;
 };
 
 struct abx_forest : abx_bvh
@@ -246,6 +255,8 @@ void destroy_tree(abx_bvh *t)
   dfree(t->sorted, s);
   dfree(t->d_bounds, s);
   dfree(t->d_off, s);
+  dfree(t->knodes, s);
+  dfree(t->kleaves, s);
   if (t->h_bounds)
   {
     if (t->ready)
@@ -361,7 +372,11 @@ abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
 
 TreeView view_of(const abx_bvh *t)
 {
-  return TreeView{t->tnodes, t->n, t->d_bounds, t->sorted, t->kind};
+  TreeView v{t->tnodes, t->n, t->d_bounds, t->sorted, t->kind};
+  v.ndir = t->ndir;
+  v.knodes = reinterpret_cast<const float *>(t->knodes);
+  v.kleaves = reinterpret_cast<const float *>(t->kleaves);
+  return v;
 }
 
 // Check a forest's query offsets (0 first, non-decreasing, one entry per
@@ -713,14 +728,52 @@ abx_status abx_profiling_reset(void)
   return ABX_SUCCESS;
 }
 
+namespace abx
+{
+// Records of a KDOP tree: (2 max(n - 1, 1) + 1) node slot records and n leaf
+// records, kdop_pad(ndir) / 4 float4 each.
+size_t kdop_node_records(int64_t n) { return n > 0 ? 2 * (size_t)std::max<int64_t>(n - 1, 1) + 1 : 1; }
+
+// A tree over n KDOP values (t->ndir set): the box tree of the values' axis
+// boxes, then the KDOP records.  An empty tree keeps one empty root record.
+abx_status build_kdop_tree(abx_bvh *t, const float *d_kdops)
+{
+  cudaStream_t s = t->stream;
+  const int64_t n = t->n;
+  const int rec = kdop_pad(t->ndir) / 4;
+  Scratch<float> boxes;
+  ABX_CUDA_TRY(boxes.alloc((size_t)std::max<int64_t>(n, 1) * 6, s));
+  ABX_TRY(kdop_axis_boxes(s, t->kdop_kind, d_kdops, n, boxes.ptr));
+  ABX_TRY(build_tree(t, boxes.ptr));
+  ABX_CUDA_TRY(dmalloc_n(&t->knodes, kdop_node_records(n) * rec, s));
+  ABX_CUDA_TRY(dmalloc_n(&t->kleaves, (size_t)std::max<int64_t>(n, 1) * rec, s));
+  if (n == 0)
+  {
+    std::vector<float> empty(4 * rec, 0.f);
+    for (int i = 0; i < t->ndir; ++i)
+    {
+      empty[i] = FLT_MAX;
+      empty[t->ndir + i] = -FLT_MAX;
+    }
+    ABX_CUDA_TRY(cudaMemcpyAsync(t->knodes, empty.data(), empty.size() * sizeof(float),
+                                 cudaMemcpyHostToDevice, s));
+    // the copy reads a host vector: finish it before returning
+    ABX_CUDA_TRY(cudaStreamSynchronize(s));
+    return ABX_SUCCESS;
+  }
+  return kdop_records(s, t->kdop_kind, t->tnodes, t->sorted, n, d_kdops, t->knodes, t->kleaves);
+}
+} // namespace abx
+
 abx_status abx_bvh_create(void *stream, abx_geometry kind, const float *d_values, int64_t n,
                           abx_bvh **out)
 {
   if (!out)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create: null output handle");
   *out = nullptr;
-  if (kind != ABX_POINT && kind != ABX_BOX)
-    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create: values must be points or boxes");
+  if (kind != ABX_POINT && kind != ABX_BOX && kdop_ndir(kind) == 0)
+    return fail(ABX_ERROR_INVALID_ARGUMENT,
+                "abx_bvh_create: values must be points, boxes or KDOPs");
   if (n < 0 || n >= (int64_t)INT32_MAX)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create: size out of range [0, 2^31-1)");
   if (n > 0 && !d_values)
@@ -731,7 +784,9 @@ abx_status abx_bvh_create(void *stream, abx_geometry kind, const float *d_values
     return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_bvh_create: host allocation");
   cudaGetDevice(&t->device);
   t->stream = as_stream(stream);
-  t->kind = kind;
+  t->kind = kdop_ndir(kind) ? ABX_BOX : kind;
+  t->ndir = kdop_ndir(kind);
+  t->kdop_kind = kind;
   t->n = n;
   cudaError_t e = cudaMallocHost(&t->h_bounds, 6 * sizeof(float));
   if (e != cudaSuccess)
@@ -747,7 +802,7 @@ abx_status abx_bvh_create(void *stream, abx_geometry kind, const float *d_values
     destroy_tree(t);
     return fail_cuda(e, "cudaEventCreate");
   }
-  abx_status st = build_tree(t, d_values);
+  abx_status st = t->ndir ? build_kdop_tree(t, d_values) : build_tree(t, d_values);
   if (st == ABX_SUCCESS)
   {
     e = cudaEventRecord(t->ready, t->stream);
@@ -770,13 +825,13 @@ abx_status abx_bvh_create_strided(void *stream, abx_geometry kind, abx_values va
   if (!out)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: null output handle");
   *out = nullptr;
-  if (kind != ABX_POINT && kind != ABX_BOX)
-    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: points or boxes");
+  if (kind != ABX_POINT && kind != ABX_BOX && kdop_ndir(kind) == 0)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: points, boxes or KDOPs");
   if (n < 0 || n >= (int64_t)INT32_MAX || values.value_stride < 0 || values.coord_stride < 0)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: bad size or strides");
   if (n > 0 && !values.data)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_create_strided: null values");
-  const int cols = kind == ABX_BOX ? 6 : 3;
+  const int cols = kdop_ndir(kind) ? 2 * kdop_ndir(kind) : kind == ABX_BOX ? 6 : 3;
   if (values.value_stride == cols && values.coord_stride == 1)
     return abx_bvh_create(stream, kind, values.data, n, out);
   cudaStream_t s = as_stream(stream);
@@ -790,6 +845,150 @@ abx_status abx_bvh_create_strided(void *stream, abx_geometry kind, abx_values va
   return abx_bvh_create(stream, kind, packed.ptr, n, out);
 }
 
+namespace
+{
+constexpr char kTreeMagic[8] = {'A', 'B', 'X', 'B', 'V', 'H', '0', '1'};
+
+struct TreeFileHeader
+{
+  char magic[8];
+  int32_t kind;
+  int32_t reserved;
+  int64_t n;
+  float bounds[6];
+};
+static_assert(sizeof(TreeFileHeader) == 48, "tree file header is 48 bytes");
+
+size_t tree_tnode_count(int64_t n) { return n > 1 ? (size_t)(n - 1) : (n == 1 ? 1 : 0); }
+size_t tree_sorted_count(abx_geometry kind, int64_t n)
+{
+  return (size_t)n * (kind == ABX_BOX ? 2 : 1);
+}
+// float4 of the KDOP records of a tree (0 for other trees)
+size_t tree_knode_count(int ndir, int64_t n)
+{
+  return ndir ? kdop_node_records(n) * (kdop_pad(ndir) / 4) : 0;
+}
+size_t tree_kleaf_count(int ndir, int64_t n)
+{
+  return ndir ? (size_t)std::max<int64_t>(n, 1) * (kdop_pad(ndir) / 4) : 0;
+}
+} // namespace
+
+abx_status abx_bvh_save(const abx_bvh *bvh, const char *path)
+{
+  if (!bvh || !path || bvh->d_off)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_save: bad argument");
+  ABX_CUDA_TRY(cudaEventSynchronize(bvh->ready));
+  TreeFileHeader h{};
+  std::memcpy(h.magic, kTreeMagic, 8);
+  h.kind = abx_bvh_geometry(bvh);
+  h.n = bvh->n;
+  std::memcpy(h.bounds, bvh->h_bounds, sizeof(h.bounds));
+  const size_t nt = tree_tnode_count(bvh->n), ns = tree_sorted_count(bvh->kind, bvh->n);
+  const size_t nkn = tree_knode_count(bvh->ndir, bvh->n), nkl = tree_kleaf_count(bvh->ndir, bvh->n);
+  std::vector<TNode> tn(nt);
+  std::vector<float4> so(ns), kn(nkn), kl(nkl);
+  if (nt)
+    ABX_CUDA_TRY(cudaMemcpy(tn.data(), bvh->tnodes, nt * sizeof(TNode), cudaMemcpyDeviceToHost));
+  if (ns)
+    ABX_CUDA_TRY(cudaMemcpy(so.data(), bvh->sorted, ns * sizeof(float4), cudaMemcpyDeviceToHost));
+  if (nkn)
+    ABX_CUDA_TRY(cudaMemcpy(kn.data(), bvh->knodes, nkn * sizeof(float4), cudaMemcpyDeviceToHost));
+  if (nkl)
+    ABX_CUDA_TRY(cudaMemcpy(kl.data(), bvh->kleaves, nkl * sizeof(float4), cudaMemcpyDeviceToHost));
+  FILE *f = std::fopen(path, "wb");
+  if (!f)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, std::string("abx_bvh_save: cannot open ") + path);
+  const bool ok = std::fwrite(&h, sizeof(h), 1, f) == 1 &&
+                  (nt == 0 || std::fwrite(tn.data(), sizeof(TNode), nt, f) == nt) &&
+                  (ns == 0 || std::fwrite(so.data(), sizeof(float4), ns, f) == ns) &&
+                  (nkn == 0 || std::fwrite(kn.data(), sizeof(float4), nkn, f) == nkn) &&
+                  (nkl == 0 || std::fwrite(kl.data(), sizeof(float4), nkl, f) == nkl);
+  const bool closed = std::fclose(f) == 0;
+  if (!ok || !closed)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, std::string("abx_bvh_save: write failed: ") + path);
+  return ABX_SUCCESS;
+}
+
+abx_status abx_bvh_load(void *stream, const char *path, abx_bvh **out)
+{
+  if (!path || !out)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_load: null argument");
+  *out = nullptr;
+  FILE *f = std::fopen(path, "rb");
+  if (!f)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, std::string("abx_bvh_load: cannot open ") + path);
+  TreeFileHeader h{};
+  bool ok = std::fread(&h, sizeof(h), 1, f) == 1 && std::memcmp(h.magic, kTreeMagic, 8) == 0 &&
+            (h.kind == ABX_POINT || h.kind == ABX_BOX || kdop_ndir(h.kind) > 0) && h.n >= 0 &&
+            h.n < (int64_t)INT32_MAX;
+  const int ndir = ok ? kdop_ndir(h.kind) : 0;
+  const abx_geometry kind = ok ? (ndir ? ABX_BOX : (abx_geometry)h.kind) : ABX_POINT;
+  const size_t nt = ok ? tree_tnode_count(h.n) : 0, ns = ok ? tree_sorted_count(kind, h.n) : 0;
+  const size_t nkn = ok ? tree_knode_count(ndir, h.n) : 0;
+  const size_t nkl = ok ? tree_kleaf_count(ndir, h.n) : 0;
+  std::vector<TNode> tn(nt);
+  std::vector<float4> so(ns), kn(nkn), kl(nkl);
+  ok = ok && (nt == 0 || std::fread(tn.data(), sizeof(TNode), nt, f) == nt) &&
+       (ns == 0 || std::fread(so.data(), sizeof(float4), ns, f) == ns) &&
+       (nkn == 0 || std::fread(kn.data(), sizeof(float4), nkn, f) == nkn) &&
+       (nkl == 0 || std::fread(kl.data(), sizeof(float4), nkl, f) == nkl);
+  std::fclose(f);
+  if (!ok)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, std::string("abx_bvh_load: not a tree file: ") + path);
+  device_state();
+  abx_bvh *t = new (std::nothrow) abx_bvh;
+  if (!t)
+    return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_bvh_load");
+  cudaGetDevice(&t->device);
+  t->stream = as_stream(stream);
+  t->kind = kind;
+  t->ndir = ndir;
+  t->kdop_kind = ndir ? (abx_geometry)h.kind : ABX_BOX;
+  t->n = h.n;
+  cudaStream_t s = t->stream;
+  cudaError_t e = cudaMallocHost(&t->h_bounds, 6 * sizeof(float));
+  if (e == cudaSuccess)
+    e = cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming);
+  if (e == cudaSuccess)
+    e = dmalloc_n(&t->d_bounds, 6, s);
+  if (e == cudaSuccess && nt)
+    e = dmalloc_n(&t->tnodes, nt, s);
+  if (e == cudaSuccess && ns)
+    e = dmalloc_n(&t->sorted, ns, s);
+  if (e == cudaSuccess && nkn)
+    e = dmalloc_n(&t->knodes, nkn, s);
+  if (e == cudaSuccess && nkl)
+    e = dmalloc_n(&t->kleaves, nkl, s);
+  if (e == cudaSuccess)
+  {
+    std::memcpy(t->h_bounds, h.bounds, sizeof(h.bounds));
+    e = cudaMemcpyAsync(t->d_bounds, t->h_bounds, 6 * sizeof(float), cudaMemcpyHostToDevice, s);
+  }
+  if (e == cudaSuccess && nt)
+    e = cudaMemcpyAsync(t->tnodes, tn.data(), nt * sizeof(TNode), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && ns)
+    e = cudaMemcpyAsync(t->sorted, so.data(), ns * sizeof(float4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && nkn)
+    e = cudaMemcpyAsync(t->knodes, kn.data(), nkn * sizeof(float4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess && nkl)
+    e = cudaMemcpyAsync(t->kleaves, kl.data(), nkl * sizeof(float4), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaEventRecord(t->ready, s);
+  // the host staging vectors are released on return: finish the copies first
+  if (e == cudaSuccess)
+    e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess)
+  {
+    cudaStreamSynchronize(s);
+    destroy_tree(t);
+    return fail_cuda(e, "abx_bvh_load");
+  }
+  *out = t;
+  return ABX_SUCCESS;
+}
+
 abx_status abx_bvh_destroy(abx_bvh *bvh)
 {
   destroy_tree(bvh);
@@ -798,7 +997,38 @@ abx_status abx_bvh_destroy(abx_bvh *bvh)
 
 int64_t abx_bvh_size(const abx_bvh *bvh) { return bvh ? bvh->n : 0; }
 
-abx_geometry abx_bvh_geometry(const abx_bvh *bvh) { return bvh ? bvh->kind : ABX_POINT; }
+abx_geometry abx_bvh_geometry(const abx_bvh *bvh)
+{
+  return bvh ? (bvh->ndir ? bvh->kdop_kind : bvh->kind) : ABX_POINT;
+}
+
+abx_status abx_bvh_kdop_bounds(const abx_bvh *bvh, float *h_kdop)
+{
+  if (!bvh || !h_kdop)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_kdop_bounds: null argument");
+  if (!bvh->ndir)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_kdop_bounds: not a KDOP tree");
+  ABX_CUDA_TRY(cudaEventSynchronize(bvh->ready));
+  const int rec = kdop_pad(bvh->ndir);
+  std::vector<float> r(rec);
+  const size_t root = (kdop_node_records(bvh->n) - 1) * rec;
+  ABX_CUDA_TRY(cudaMemcpy(r.data(), reinterpret_cast<const float *>(bvh->knodes) + root,
+                          rec * sizeof(float), cudaMemcpyDeviceToHost));
+  std::memcpy(h_kdop, r.data(), 2 * bvh->ndir * sizeof(float));
+  return ABX_SUCCESS;
+}
+
+abx_status abx_kdop_from_geometry(void *stream, abx_geometry kind, const float *d_values,
+                                  int64_t n, abx_geometry kdop_kind, float *d_kdops)
+{
+  if ((kind != ABX_POINT && kind != ABX_BOX) || kdop_ndir(kdop_kind) == 0)
+    return fail(ABX_ERROR_INVALID_ARGUMENT,
+                "abx_kdop_from_geometry: points or boxes to a KDOP kind");
+  if (n < 0 || (n > 0 && (!d_values || !d_kdops)))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_kdop_from_geometry: bad arrays");
+  device_state();
+  return kdop_from_geometry(as_stream(stream), kind, d_values, n, kdop_kind, d_kdops);
+}
 
 abx_status abx_bvh_bounds(const abx_bvh *bvh, float h_box[6])
 {
@@ -816,6 +1046,8 @@ abx_status abx_bvh_export_nodes(const abx_bvh *bvh, void *stream, int32_t *d_lea
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_export_nodes: null tree");
   cudaStream_t s = as_stream(stream);
   ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+  if (bvh->ndir)
+    return fail(ABX_ERROR_NOT_SUPPORTED, "abx_bvh_export_nodes: KDOP-bounded tree");
   if (!d_leaves && !d_internal)
     return ABX_SUCCESS;
   device_state();
@@ -828,6 +1060,8 @@ abx_status abx_bvh_device_view(const abx_bvh *bvh, abx_device_view *out)
 {
   if (!bvh || !out)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_device_view: null argument");
+  if (bvh->ndir)
+    return fail(ABX_ERROR_NOT_SUPPORTED, "abx_bvh_device_view: KDOP-bounded tree");
   out->nodes = bvh->tnodes;
   out->leaves = bvh->sorted;
   out->size = bvh->n;
@@ -845,9 +1079,13 @@ abx_status abx_bvh_query_intersects(const abx_bvh *bvh, void *stream, abx_geomet
   *out = nullptr;
   if (bvh->d_off)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: a forest handle");
-  if (kind != ABX_SPHERE && kind != ABX_BOX && kind != ABX_RAY)
+  if (kind != ABX_SPHERE && kind != ABX_BOX && kind != ABX_RAY && kdop_ndir(kind) == 0)
     return fail(ABX_ERROR_INVALID_ARGUMENT,
-                "abx_bvh_query_intersects: predicates must be spheres, boxes or rays");
+                "abx_bvh_query_intersects: predicates must be spheres, boxes, rays or KDOPs");
+  if (bvh->ndir && kind != ABX_BOX && kdop_ndir(kind) != bvh->ndir)
+    return fail(ABX_ERROR_INVALID_ARGUMENT,
+                "abx_bvh_query_intersects: a KDOP tree answers intersects(Box) and "
+                "intersects(KDOP) with its own directions");
   if (nq < 0 || nq >= (int64_t)INT32_MAX)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_intersects: bad number of queries");
   if (nq > 0 && !d_predicates)
@@ -874,6 +1112,9 @@ abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream, const float *
   *out = nullptr;
   if (bvh->d_off)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: a forest handle");
+  if (bvh->ndir)
+    return fail(ABX_ERROR_INVALID_ARGUMENT,
+                "abx_bvh_query_nearest: no distance to a KDOP (nearest queries need points or boxes)");
   if (nq < 0 || nq >= (int64_t)INT32_MAX)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest: bad number of queries");
   if (nq > 0 && !d_queries)
@@ -890,6 +1131,8 @@ abx_status abx_bvh_query_nearest_into(const abx_bvh *bvh, void *stream, const fl
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: null argument");
   if (bvh->d_off)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: a forest handle");
+  if (bvh->ndir)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: no distance to a KDOP");
   if (nq < 0 || nq >= (int64_t)INT32_MAX || (nq > 0 && !d_queries))
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_nearest_into: bad queries");
   cudaStream_t s = as_stream(stream);
@@ -931,6 +1174,9 @@ abx_status abx_bvh_query_ordered_intersects(const abx_bvh *bvh, void *stream, co
   *out = nullptr;
   if (bvh->d_off)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_ordered_intersects: a forest handle");
+  if (bvh->ndir)
+    return fail(ABX_ERROR_INVALID_ARGUMENT,
+                "abx_bvh_query_ordered_intersects: no ray test for KDOP values");
   if (nq < 0 || nq >= (int64_t)INT32_MAX || (nq > 0 && !d_rays))
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_bvh_query_ordered_intersects: bad rays");
   cudaStream_t s = as_stream(stream);
@@ -1098,9 +1344,9 @@ abx_status abx_forest_query_intersects(const abx_forest *forest, void *stream,
   if (!forest || !out)
     return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_forest_query_intersects: null argument");
   *out = nullptr;
-  if (kind != ABX_SPHERE && kind != ABX_BOX)
+  if (kind != ABX_SPHERE && kind != ABX_BOX && kdop_ndir(kind) == 0)
     return fail(ABX_ERROR_INVALID_ARGUMENT,
-                "abx_forest_query_intersects: predicates must be spheres or boxes");
+                "abx_forest_query_intersects: predicates must be spheres, boxes or KDOPs");
   ABX_TRY(check_query_offsets(forest, h_query_offsets, "abx_forest_query_intersects"));
   const int64_t nq = h_query_offsets[forest->ntrees];
   if (nq > 0 && !d_predicates)

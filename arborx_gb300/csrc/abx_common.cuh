@@ -267,10 +267,30 @@ __device__ __forceinline__ uint32_t morton32_unit(float x, float y, float z)
 // Geometry access
 // ---------------------------------------------------------------------------
 
-// Centroid of a value (geometry/algorithms/ArborX_Centroid.hpp:40-60).
+// Centroid of a value (geometry/algorithms/ArborX_Centroid.hpp:40-60).  The
+// general form takes the KDOP kinds 4..7 (2 * ndir floats each): the centroid
+// of the KDOP's axis box, Box{} expanded by the first three directions'
+// ranges (ArborX_Centroid.hpp:84-94).
 template <int KIND>
 __device__ __forceinline__ void load_centroid(const float *g, int64_t i, float &x,
-                                              float &y, float &z);
+                                              float &y, float &z)
+{
+  static_assert(KIND >= 4 && KIND <= 7, "geometry kind");
+  constexpr int nd = KIND == 4 ? 3 : KIND == 5 ? 7 : KIND == 6 ? 9 : 13;
+  const float *k = g + 2 * nd * i;
+  float c[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+  {
+    const float mn = __ldg(k + d), mx = __ldg(k + nd + d);
+    const float lo = mn < FLT_MAX ? mn : FLT_MAX;
+    const float hi = -FLT_MAX < mx ? mx : -FLT_MAX;
+    c[d] = __fdiv_rn(__fadd_rn(lo, hi), 2.f);
+  }
+  x = c[0];
+  y = c[1];
+  z = c[2];
+}
 
 // KIND: 0 point (3 floats), 1 box (6 floats), 2 sphere (4 floats).
 template <>

@@ -941,18 +941,24 @@ abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const floa
   while ((1ll << tree_bits) < nseg)
     ++tree_bits;
   const unsigned blocks = (unsigned)((nq + 255) / 256);
+#define ABX_QK(KIND, KEY)                                                                      \
+  k_forest_query_keys<KIND, KEY><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, tree_bits, nq,   \
+                                                       d_bounds, keys.ptr)
 #define ABX_QKEYS(KEY)                                                                        \
   do                                                                                          \
   {                                                                                           \
-    if (pred_kind == ABX_POINT)                                                               \
-      k_forest_query_keys<0, KEY><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, tree_bits, nq, \
-                                                        d_bounds, keys.ptr);                  \
-    else if (pred_kind == ABX_BOX)                                                            \
-      k_forest_query_keys<1, KEY><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, tree_bits, nq, \
-                                                        d_bounds, keys.ptr);                  \
-    else                                                                                      \
-      k_forest_query_keys<2, KEY><<<blocks, 256, 0, s>>>(d_preds, d_qoff, nseg, tree_bits, nq, \
-                                                        d_bounds, keys.ptr);                  \
+    switch (pred_kind)                                                                        \
+    {                                                                                         \
+    case ABX_POINT: ABX_QK(0, KEY); break;                                                    \
+    case ABX_BOX: ABX_QK(1, KEY); break;                                                      \
+    case ABX_SPHERE: ABX_QK(2, KEY); break;                                                   \
+    case ABX_RAY: ABX_QK(3, KEY); break;                                                      \
+    case ABX_KDOP6: ABX_QK(4, KEY); break;                                                    \
+    case ABX_KDOP14: ABX_QK(5, KEY); break;                                                   \
+    case ABX_KDOP18: ABX_QK(6, KEY); break;                                                   \
+    case ABX_KDOP26: ABX_QK(7, KEY); break;                                                   \
+    default: return fail(ABX_ERROR_INVALID_ARGUMENT, "predicate kind");                       \
+    }                                                                                         \
     ABX_CUDA_TRY(cudaGetLastError());                                                         \
   } while (0)
   if (tree_bits <= 16)
@@ -967,6 +973,7 @@ abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const floa
   ABX_CUDA_TRY(keys.alloc(nq, s));
   ABX_QKEYS(uint64_t);
 #undef ABX_QKEYS
+#undef ABX_QK
   return radix_sort_u64(s, keys.ptr, d_perm, nullptr, nq, (32 + tree_bits + 7) / 8, nullptr);
 }
 

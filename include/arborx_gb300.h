@@ -68,7 +68,15 @@ typedef enum abx_geometry
   ABX_POINT = 0,
   ABX_BOX = 1,
   ABX_SPHERE = 2,
-  ABX_RAY = 3
+  ABX_RAY = 3,
+  /* Discrete oriented polytopes KDOP<3, k> (src/geometry/ArborX_KDOP.hpp:
+   * 64-183), k/2 directions: the axes, for k = 18 and 26 the edge
+   * directions, for k = 14 and 26 the corner directions, in the reference's
+   * order.  One KDOP is 2 * (k/2) floats: min[k/2] then max[k/2]. */
+  ABX_KDOP6 = 4,
+  ABX_KDOP14 = 5,
+  ABX_KDOP18 = 6,
+  ABX_KDOP26 = 7
 } abx_geometry;
 
 /* TraversalPolicy (src/spatial/detail/ArborX_TraversalPolicy.hpp:19-47):
@@ -155,6 +163,39 @@ typedef struct abx_values
 
 ABX_API abx_status abx_bvh_create_strided(void *stream, abx_geometry kind, abx_values values,
                                           int64_t n, abx_bvh **out);
+
+/* KDOP bounding volumes (src/geometry/ArborX_KDOP.hpp; the BoundingVolume
+ * parameter of BoundingVolumeHierarchy, src/spatial/ArborX_LinearBVH.hpp:
+ * 56-60).  abx_bvh_create with kind ABX_KDOP6/14/18/26 builds a tree over n
+ * KDOP values (2 * (k/2) floats each) whose nodes are bounded by KDOPs of
+ * the same directions; it answers intersects(Box) and intersects(KDOP of the
+ * same k) predicates (abx_bvh_query_intersects), with the reference's
+ * KDOP-box and KDOP-KDOP tests (ArborX_Intersects.hpp:317-368).  KDOP
+ * predicates (kind ABX_KDOPk, any k) also run on point and box trees and on
+ * brute force.  The reference defines no distance to a KDOP and no
+ * sphere- or ray-KDOP test: nearest, sphere and ray queries on a KDOP tree
+ * return ABX_ERROR_INVALID_ARGUMENT.  Forests and BruteForce take points and
+ * boxes only.
+ *
+ * abx_kdop_from_geometry: KDOP{} expanded by each of n points or boxes
+ * (ArborX_Expand.hpp:128-208), written to d_kdops (device, 2 * (k/2) floats
+ * per value): the conversion the reference's test trees apply to their
+ * primitives (test/ArborXTest_LegacyTree.hpp:50-60).
+ * abx_bvh_kdop_bounds: the KDOP of the whole tree (bounds() of a KDOP-bounded
+ * tree), 2 * (k/2) floats to host memory; waits for the build. */
+ABX_API abx_status abx_kdop_from_geometry(void *stream, abx_geometry kind, const float *d_values,
+                                          int64_t n, abx_geometry kdop_kind, float *d_kdops);
+ABX_API abx_status abx_bvh_kdop_bounds(const abx_bvh *bvh, float *h_kdop);
+
+/* On-disk trees (warm restarts of a serving process; no counterpart in the
+ * reference).  abx_bvh_save writes the tree (geometry kind, size, bounds,
+ * child-pair nodes, Morton-ordered leaves, and for KDOP trees the KDOP
+ * records) to `path`; abx_bvh_load reads it back to the current device: the
+ * loaded tree answers every query exactly like the saved one.  The file
+ * starts with the 8 bytes "ABXBVH01" followed by little-endian int32 kind,
+ * int32 reserved, int64 size, float bounds[6], then the arrays. */
+ABX_API abx_status abx_bvh_save(const abx_bvh *bvh, const char *path);
+ABX_API abx_status abx_bvh_load(void *stream, const char *path, abx_bvh **out);
 
 /* Destroy a tree (frees stream-ordered on the stream it was built on). */
 ABX_API abx_status abx_bvh_destroy(abx_bvh *bvh);

@@ -1327,3 +1327,184 @@ int64_t abxo_ray_brute(const float *geom, int64_t n, int is_box, const float *ra
   free(hits);
   return total;
 }
+
+/* ---------------------------------------------------------------------------
+ * KDOP<3, k> bounding volumes (src/geometry/ArborX_KDOP.hpp:30-183).  A KDOP
+ * with ndir = k/2 directions is 2 * ndir floats: min[ndir] then max[ndir].
+ * ------------------------------------------------------------------------- */
+
+/* Directions, ArborX_KDOP.hpp:64-151: axes; for k = 18, 26 the edges; for
+ * k = 14, 26 the corners. */
+static const signed char kdop_axes[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+static const signed char kdop_edges[6][3] = {{1, 1, 0}, {1, 0, 1}, {0, 1, 1},
+                                             {1, -1, 0}, {1, 0, -1}, {0, 1, -1}};
+static const signed char kdop_corners[4][3] = {{1, 1, 1}, {1, -1, 1}, {1, 1, -1}, {1, -1, -1}};
+
+static const signed char *kdop_direction(int ndir, int i)
+{
+  if (i < 3)
+    return kdop_axes[i];
+  if (ndir == 7)
+    return kdop_corners[i - 3];
+  if (i < 9)
+    return kdop_edges[i - 3];
+  return kdop_corners[i - 9];
+}
+
+/* proj_i = point[0] * dir[0]; proj_i += point[d] * dir[d]
+ * (ArborX_Expand.hpp:136-140, ArborX_Intersects.hpp:336-340). */
+static float kdop_proj(int ndir, int i, const float *p)
+{
+  const signed char *d = kdop_direction(ndir, i);
+  float proj = p[0] * (float)d[0];
+  proj += p[1] * (float)d[1];
+  proj += p[2] * (float)d[2];
+  return proj;
+}
+
+/* KDOP() (ArborX_KDOP.hpp:164-172). */
+void abxo_kdop_empty(int ndir, float *k)
+{
+  for (int i = 0; i < ndir; ++i)
+  {
+    k[i] = FLT_MAX;
+    k[ndir + i] = -FLT_MAX;
+  }
+}
+
+/* expand(KDOP, Point) (ArborX_Expand.hpp:128-148). */
+void abxo_kdop_expand_point(int ndir, float *k, const float *p)
+{
+  for (int i = 0; i < ndir; ++i)
+  {
+    const float proj = kdop_proj(ndir, i, p);
+    k[i] = kmin(k[i], proj);
+    k[ndir + i] = kmax(k[ndir + i], proj);
+  }
+}
+
+/* expand(KDOP, Box) (ArborX_Expand.hpp:151-208): an inverted range leaves the
+ * KDOP unchanged; else the eight corners in the reference's order. */
+void abxo_kdop_expand_box(int ndir, float *k, const float *b)
+{
+  for (int d = 0; d < 3; ++d)
+    if (b[d] > b[3 + d])
+      return;
+  const float xs[2] = {b[0], b[3]}, ys[2] = {b[1], b[4]}, zs[2] = {b[2], b[5]};
+  const int order[8][3] = {{0, 0, 0}, {0, 1, 0}, {0, 0, 1}, {0, 1, 1},
+                           {1, 0, 0}, {1, 1, 0}, {1, 0, 1}, {1, 1, 1}};
+  for (int c = 0; c < 8; ++c)
+  {
+    const float p[3] = {xs[order[c][0]], ys[order[c][1]], zs[order[c][2]]};
+    abxo_kdop_expand_point(ndir, k, p);
+  }
+}
+
+/* intersects(KDOP, KDOP) (ArborX_Intersects.hpp:350-368). */
+int abxo_kdop_intersects_kdop(int ndir, const float *kdop, const float *other)
+{
+  for (int i = 0; i < ndir; ++i)
+    if (other[ndir + i] < kdop[i] || other[i] > kdop[ndir + i])
+      return 0;
+  return 1;
+}
+
+/* intersects(KDOP, Box) (ArborX_Intersects.hpp:317-326). */
+int abxo_kdop_intersects_box(int ndir, const float *kdop, const float *box)
+{
+  float other[26];
+  abxo_kdop_empty(ndir, other);
+  abxo_kdop_expand_box(ndir, other, box);
+  return abxo_kdop_intersects_kdop(ndir, kdop, other);
+}
+
+/* intersects(Point, KDOP) (ArborX_Intersects.hpp:328-348). */
+int abxo_point_intersects_kdop(int ndir, const float *p, const float *kdop)
+{
+  for (int i = 0; i < ndir; ++i)
+  {
+    const float proj = kdop_proj(ndir, i, p);
+    if (proj < kdop[i] || proj > kdop[ndir + i])
+      return 0;
+  }
+  return 1;
+}
+
+/* KDOP{} expanded by each point (is_box 0) or box (is_box 1). */
+void abxo_kdop_from_geometry(int ndir, int is_box, const float *g, int64_t n, float *out)
+{
+  for (int64_t i = 0; i < n; ++i)
+  {
+    float *k = out + 2 * ndir * i;
+    abxo_kdop_empty(ndir, k);
+    if (is_box)
+      abxo_kdop_expand_box(ndir, k, g + 6 * i);
+    else
+      abxo_kdop_expand_point(ndir, k, g + 3 * i);
+  }
+}
+
+/* Box{} expanded by each KDOP (expand(Box, KDOP), ArborX_Expand.hpp:210-225,
+ * through expand(Box, Box), :60-77): the ranges of the three axes. */
+void abxo_kdop_axis_boxes(int ndir, const float *kd, int64_t n, float *boxes)
+{
+  for (int64_t i = 0; i < n; ++i)
+    for (int d = 0; d < 3; ++d)
+    {
+      boxes[6 * i + d] = kmin(FLT_MAX, kd[2 * ndir * i + d]);
+      boxes[6 * i + 3 + d] = kmax(-FLT_MAX, kd[2 * ndir * i + ndir + d]);
+    }
+}
+
+/* One value-predicate test.  vkind/pkind: 0 point, 1 box, 2 KDOP (vndir /
+ * pndir directions).  intersects is symmetric through reverse dispatch
+ * (algorithms/ArborX_ReverseDispatch.hpp). */
+static int kdop_leaf_test(int vkind, int vndir, const float *v, int pkind, int pndir,
+                          const float *p)
+{
+  if (pkind == 1 && vkind == 0) /* intersects(Point, Box), Intersects.hpp:67-80 */
+  {
+    for (int d = 0; d < 3; ++d)
+      if (v[d] < p[d] || v[d] > p[3 + d])
+        return 0;
+    return 1;
+  }
+  if (pkind == 1 && vkind == 1) /* intersects(Box, Box), Intersects.hpp:51-65 */
+  {
+    for (int d = 0; d < 3; ++d)
+      if (p[d] > v[3 + d] || p[3 + d] < v[d])
+        return 0;
+    return 1;
+  }
+  if (pkind == 1 && vkind == 2)
+    return abxo_kdop_intersects_box(vndir, v, p);
+  if (pkind == 2 && vkind == 0)
+    return abxo_point_intersects_kdop(pndir, v, p);
+  if (pkind == 2 && vkind == 1)
+    return abxo_kdop_intersects_box(pndir, p, v);
+  return abxo_kdop_intersects_kdop(pndir, p, v);
+}
+
+/* Every predicate against every value, matches in ascending value order
+ * (indices may be null: counts only).  Returns the number of matches. */
+int64_t abxo_kdop_spatial_brute(const float *values, int64_t n, int vkind, int vndir,
+                                const float *preds, int64_t nq, int pkind, int pndir,
+                                int32_t *offsets, int32_t *indices)
+{
+  const int vs = vkind == 0 ? 3 : vkind == 1 ? 6 : 2 * vndir;
+  const int ps = pkind == 1 ? 6 : 2 * pndir;
+  int64_t total = 0;
+  offsets[0] = 0;
+  for (int64_t q = 0; q < nq; ++q)
+  {
+    for (int64_t i = 0; i < n; ++i)
+      if (kdop_leaf_test(vkind, vndir, values + vs * i, pkind, pndir, preds + ps * q))
+      {
+        if (indices)
+          indices[total] = (int32_t)i;
+        ++total;
+      }
+    offsets[q + 1] = (int32_t)total;
+  }
+  return total;
+}

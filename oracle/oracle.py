@@ -77,6 +77,17 @@ def lib():
         L.abxo_spatial_brute.restype = I64
         L.abxo_spatial_brute.argtypes = [P, I64, I, I, P, I64, P, P]
         L.abxo_exclusive_scan_i32.argtypes = [P, I64, P]
+        for name in ("abxo_kdop_empty",):
+            getattr(L, name).argtypes = [I, P]
+        L.abxo_kdop_expand_point.argtypes = [I, P, P]
+        L.abxo_kdop_expand_box.argtypes = [I, P, P]
+        L.abxo_kdop_intersects_kdop.argtypes = [I, P, P]
+        L.abxo_kdop_intersects_box.argtypes = [I, P, P]
+        L.abxo_point_intersects_kdop.argtypes = [I, P, P]
+        L.abxo_kdop_from_geometry.argtypes = [I, I, P, I64, P]
+        L.abxo_kdop_axis_boxes.argtypes = [I, P, I64, P]
+        L.abxo_kdop_spatial_brute.restype = I64
+        L.abxo_kdop_spatial_brute.argtypes = [P, I64, I, I, P, I64, I, I, P, P]
         L.abxo_visit_counts.argtypes = [I64, I, P, P, P, I, I, P, I64, I32, P, P]
         L.abxo_ray_normalize.argtypes = [P, I64, P]
         L.abxo_ray_box_intersection.restype = I
@@ -319,3 +330,90 @@ def spatial_brute(geom, kind, preds, is_box=False):
     indices = np.empty(total, np.int32)
     lib().abxo_spatial_brute(_p(g), g.shape[0], int(is_box), int(kind), _p(p), nq, _p(offsets), _p(indices))
     return offsets, indices
+
+
+# ---------------------------------------------------------------------------
+# KDOP<3, k> (src/geometry/ArborX_KDOP.hpp): ndir = k/2 directions, a KDOP is
+# 2 * ndir float32 (min[ndir] then max[ndir]).
+# ---------------------------------------------------------------------------
+
+KDOP_NDIR = {6: 3, 14: 7, 18: 9, 26: 13}
+
+
+def kdop_empty(ndir):
+    k = np.empty(2 * ndir, np.float32)
+    lib().abxo_kdop_empty(ndir, _p(k))
+    return k
+
+
+def kdop_expand(k, geom):
+    """expand(KDOP, Point) for a 3-vector, expand(KDOP, Box) for a 6-vector;
+    k is updated in place and returned."""
+    ndir = k.size // 2
+    g = np.ascontiguousarray(geom, np.float32)
+    if g.size == 3:
+        lib().abxo_kdop_expand_point(ndir, _p(k), _p(g))
+    else:
+        lib().abxo_kdop_expand_box(ndir, _p(k), _p(g))
+    return k
+
+
+def kdop_intersects(k, other):
+    """intersects(KDOP, Point | Box | KDOP) (symmetric)."""
+    ndir = k.size // 2
+    o = np.ascontiguousarray(other, np.float32)
+    if o.size == 3:
+        return bool(lib().abxo_point_intersects_kdop(ndir, _p(o), _p(k)))
+    if o.size == 6 and ndir != 3:
+        return bool(lib().abxo_kdop_intersects_box(ndir, _p(k), _p(o)))
+    return bool(lib().abxo_kdop_intersects_kdop(ndir, _p(k), _p(o)))
+
+
+def kdop_from_geometry(geom, ndir, is_box=False):
+    g = _f32(geom, 6 if is_box else 3)
+    out = np.empty((g.shape[0], 2 * ndir), np.float32)
+    lib().abxo_kdop_from_geometry(ndir, int(is_box), _p(g), g.shape[0], _p(out))
+    return out
+
+
+def kdop_axis_boxes(kdops):
+    k = np.ascontiguousarray(kdops, np.float32)
+    ndir = k.shape[1] // 2
+    out = np.empty((k.shape[0], 6), np.float32)
+    lib().abxo_kdop_axis_boxes(ndir, _p(k), k.shape[0], _p(out))
+    return out
+
+
+def kdop_spatial_brute(values, vkind, preds, pkind):
+    """CRS of intersects over every value, ascending values per row.  vkind /
+    pkind: "point", "box" or a KDOP k (6, 14, 18, 26)."""
+    def code(kind):
+        if kind == "point":
+            return 0, 0, 3
+        if kind == "box":
+            return 1, 0, 6
+        return 2, KDOP_NDIR[kind], 2 * KDOP_NDIR[kind]
+    vk, vn, vs = code(vkind)
+    pk, pn, ps = code(pkind)
+    v = _f32(values, vs)
+    p = _f32(preds, ps)
+    nq = p.shape[0]
+    offsets = np.zeros(nq + 1, np.int32)
+    total = lib().abxo_kdop_spatial_brute(_p(v), v.shape[0], vk, vn, _p(p), nq, pk, pn, _p(offsets), None)
+    indices = np.empty(total, np.int32)
+    lib().abxo_kdop_spatial_brute(_p(v), v.shape[0], vk, vn, _p(p), nq, pk, pn, _p(offsets), _p(indices))
+    return offsets, indices
+
+
+def in_tree_order(offsets, indices, leaf_values):
+    """Each CRS row reordered by the leaves' Morton positions (leaf_values:
+    the tree's leaf values in Morton order): the order of a depth-first,
+    left-first traversal, whatever its pruning."""
+    pos = np.empty(len(leaf_values), np.int64)
+    pos[np.asarray(leaf_values)] = np.arange(len(leaf_values))
+    out = indices.copy()
+    for q in range(len(offsets) - 1):
+        a, b = offsets[q], offsets[q + 1]
+        row = indices[a:b]
+        out[a:b] = row[np.argsort(pos[row], kind="stable")]
+    return out

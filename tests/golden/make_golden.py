@@ -212,6 +212,60 @@ def rays(root):
                             "indices": [0]}}
 
 
+
+def kdops(root):
+    """test/tstGeometryIntersects.cpp:384-571 (KDOP<3, k> for k = 6, 14, 18,
+    26: KDOP-KDOP and KDOP-box against the empty KDOP / box, and the two
+    point-KDOP polytopes with their per-k expected answers) and
+    test/tstQueryTreeIntersectsKDOP.cpp:26-91 (13 points, a KDOP<3, 18>
+    predicate; empty predicate list).  Points in each polytope are the
+    expand() calls in order."""
+    src = _read(root, "test/tstGeometryIntersects.cpp")
+    body = src[src.index("BOOST_AUTO_TEST_CASE_TEMPLATE(intersects_point_kdop, KDOP_t, KDOP_3D_types)"):]
+    body = body[:body.index("\n}\n") + 3]
+    flat = re.sub(r"\s+", " ", body)
+    blocks = flat.split("KDOP_t x;")[1:]
+    num = r"[-0-9.]+"
+    pt = r"Point\{(%s), (%s), (%s)\}" % (num, num, num)
+    polytopes = []
+    for blk in blocks:
+        expands = [[float(v) for v in m] for m in re.findall(r"expand\(x, " + pt + r"\);", blk)]
+        checks = []
+        for neg, x, y, z, cond in re.findall(
+                r"BOOST_TEST\((!?)sym_intersects\(" + pt + r", x\)(?: == \(?([a-z_0-9| ]+)\)?)?\);", blk):
+            expect = {}
+            for k, flag in ((6, "is_kdop_3_6"), (14, "is_kdop_3_14"), (18, "is_kdop_3_18"), (26, None)):
+                if cond:
+                    val = any(c.strip() == flag for c in cond.split("||"))
+                else:
+                    val = neg == ""
+                expect[str(k)] = val
+            checks.append({"point": [float(x), float(y), float(z)], "expected": expect})
+        polytopes.append({"expand": expands, "checks": checks})
+    assert [blk.count("sym_intersects(") for blk in blocks] == [len(p["checks"]) for p in polytopes]
+    assert [(len(p["expand"]), len(p["checks"])) for p in polytopes] == [(0, 1), (10, 9), (9, 9)]
+    qsrc = _read(root, "test/tstQueryTreeIntersectsKDOP.cpp")
+    prims = [[float(v) for v in m] for m in re.findall(r"\{\{(%s), (%s), (%s)\}\}, // \d+" % (num, num, num), qsrc)]
+    qexp = [[float(v) for v in m] for m in re.findall(r"expand\(x, " + pt + r"\);", qsrc)]
+    sol = re.findall(r"make_reference_solution<int>\(\{([0-9, ]*)\}, \{([0-9, ]*)\}\)", qsrc)
+    ints = lambda t: [int(v) for v in t.replace(" ", "").split(",") if v]
+    assert len(prims) == 13 and len(qexp) == 10 and len(sol) == 2, (len(prims), len(qexp), sol)
+    unit = [[1, 0, 0], [0, 1, 0], [0, 0, 1]]
+    return {"cite": "test/tstGeometryIntersects.cpp:384-571, test/tstQueryTreeIntersectsKDOP.cpp:26-91",
+            # intersects_kdop_kdop_3D / intersects_kdop_box_3D (:440-472): the
+            # empty KDOP meets nothing; after expanding by the three unit
+            # points it meets itself and the unit box, never an empty KDOP or
+            # the empty Box{}
+            "kdop_kdop": {"expand": unit, "self_before": False, "self_after": True,
+                          "empty_after": False},
+            "kdop_box": {"expand": unit, "unit_box": [0, 0, 0, 1, 1, 1],
+                         "before": {"empty": False, "unit": False},
+                         "after": {"empty": False, "unit": True}},
+            "point_kdop": polytopes,
+            "tree": {"points": prims, "kdop18_expand": qexp,
+                     "empty": {"indices": ints(sol[0][0]), "offsets": ints(sol[0][1])},
+                     "query": {"indices": ints(sol[1][0]), "offsets": ints(sol[1][1])}}}
+
 def main(root):
     data = {
         "source": "ArborX 2.1.99 test sources (read as text)",
@@ -222,6 +276,7 @@ def main(root):
         "crs_query_impl": crs_query_impl(),
         "neighbor_lists": neighbor_lists(root),
         "rays": rays(root),
+        "kdops": kdops(root),
         "stack_capacity": {"cite": "tstQueryTreeDegenerate.cpp:367-446", "n": 4096},
         "manufactured_grid": {"cite": "tstQueryTreeManufacturedSolution.cpp:64-269", "nx": 11, "L": 100.0},
     }

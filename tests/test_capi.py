@@ -66,3 +66,24 @@ def test_forest_arguments_are_checked_on_the_host():
     assert L.abx_forest_create(None, 0, None, o.ctypes.data, 0, ctypes.byref(h)) == 1
     assert L.abx_forest_create(None, 2, None, o.ctypes.data, 0, ctypes.byref(h)) == 1
     assert L.abx_forest_num_trees(None) == 0 and L.abx_forest_size(None, 0) == 0
+
+
+def test_tree_file_errors_are_reported_on_the_host(tmp_path):
+    """abx_bvh_load refuses a missing file and a file that is not a tree
+    before any device work."""
+    import ctypes
+
+    from arborx_gb300 import _lib
+
+    L = _lib.load()
+    h = ctypes.c_void_p()
+    missing = str(tmp_path / "missing.abx").encode()
+    assert L.abx_bvh_load(None, missing, ctypes.byref(h)) == 1
+    assert not h.value
+    bad = tmp_path / "bad.abx"
+    bad.write_bytes(b"ABXBVH01" + b"\0" * 8)  # header cut short
+    assert L.abx_bvh_load(None, str(bad).encode(), ctypes.byref(h)) == 1
+    bad.write_bytes(b"NOTATREE" + b"\0" * 64)
+    assert L.abx_bvh_load(None, str(bad).encode(), ctypes.byref(h)) == 1
+    assert not h.value
+    assert L.abx_bvh_save(None, missing) == 1

@@ -242,3 +242,66 @@ def test_oracle_ray_tree_cases_golden(golden):
     off, ind, _ = o.ray_brute(np.asarray([one["box"]], np.float32),
                               o.ray_normalize(np.asarray(one["rays"], np.float32)), ordered=True)
     assert off.tolist() == one["offsets"] and ind.tolist() == one["indices"]
+
+
+@pytest.mark.parametrize("k", [6, 14, 18, 26])
+def test_oracle_kdop_geometry_golden(golden, k):
+    """test/tstGeometryIntersects.cpp:384-571: KDOP-KDOP and KDOP-box against
+    empty operands, and the per-k answers of points against a unit cube with
+    an edge or a corner cut off."""
+    g = golden["kdops"]
+    nd = o.KDOP_NDIR[k]
+    x = o.kdop_empty(nd)
+    assert o.kdop_intersects(x, x) == g["kdop_kdop"]["self_before"]
+    unit = np.asarray(g["kdop_box"]["unit_box"], np.float32)
+    empty_box = np.array([np.finfo(np.float32).max] * 3 + [-np.finfo(np.float32).max] * 3, np.float32)
+    assert o.kdop_intersects(x, empty_box) == g["kdop_box"]["before"]["empty"]
+    assert o.kdop_intersects(x, unit) == g["kdop_box"]["before"]["unit"]
+    for p in g["kdop_kdop"]["expand"]:
+        o.kdop_expand(x, p)
+    assert o.kdop_intersects(x, x) == g["kdop_kdop"]["self_after"]
+    assert o.kdop_intersects(x, o.kdop_empty(nd)) == g["kdop_kdop"]["empty_after"]
+    assert o.kdop_intersects(x, empty_box) == g["kdop_box"]["after"]["empty"]
+    assert o.kdop_intersects(x, unit) == g["kdop_box"]["after"]["unit"]
+    for poly in g["point_kdop"]:
+        x = o.kdop_empty(nd)
+        for p in poly["expand"]:
+            o.kdop_expand(x, p)
+        for c in poly["checks"]:
+            assert o.kdop_intersects(x, c["point"]) == c["expected"][str(k)], (k, c)
+
+
+def test_oracle_kdop_query_golden(golden):
+    """test/tstQueryTreeIntersectsKDOP.cpp:26-91: intersects(KDOP<3, 18>) over
+    13 points finds {1, 4, 7, 8}; no predicates give offsets {0}."""
+    t = golden["kdops"]["tree"]
+    x = o.kdop_empty(9)
+    for p in t["kdop18_expand"]:
+        o.kdop_expand(x, p)
+    pts = np.asarray(t["points"], np.float32)
+    off, ind = o.kdop_spatial_brute(pts, "point", x[None], 18)
+    assert off.tolist() == t["query"]["offsets"] and sorted(ind.tolist()) == t["query"]["indices"]
+    off, ind = o.kdop_spatial_brute(pts, "point", np.zeros((0, 18), np.float32), 18)
+    assert off.tolist() == t["empty"]["offsets"] and ind.tolist() == t["empty"]["indices"]
+
+
+def test_oracle_kdop_conversions():
+    """A point's KDOP has zero-width ranges at its projections; a box's KDOP
+    holds each of its corners and the box's own ranges on the axes; the axis
+    boxes of those KDOPs give the boxes back (expand(Box, KDOP))."""
+    rng = np.random.default_rng(5)
+    lo = rng.random((200, 3), dtype=np.float32)
+    boxes = np.concatenate([lo, lo + rng.random((200, 3), dtype=np.float32)], axis=1)
+    for k, nd in o.KDOP_NDIR.items():
+        kb = o.kdop_from_geometry(boxes, nd, is_box=True)
+        assert np.array_equal(o.kdop_axis_boxes(kb), boxes)
+        kp = o.kdop_from_geometry(lo, nd)
+        assert np.array_equal(kp[:, :nd], kp[:, nd:])
+        assert np.array_equal(kp[:, :3], lo)
+        for i in range(0, 200, 37):
+            for c in range(8):
+                corner = [boxes[i, 3 * ((c >> 2) & 1)], boxes[i, 1 + 3 * (c & 1)], boxes[i, 2 + 3 * ((c >> 1) & 1)]]
+                assert o.kdop_intersects(kb[i], corner)
+    # an inverted box leaves the KDOP empty (ArborX_Expand.hpp:163-165)
+    bad = np.array([[1, 0, 0, 0, 1, 1]], np.float32)
+    assert np.array_equal(o.kdop_from_geometry(bad, 7, is_box=True)[0], o.kdop_empty(7))
