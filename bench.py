@@ -70,7 +70,10 @@ def parse():
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[500, 2000, 8000, 32000])
     ap.add_argument("--clouds", type=int, default=4096,
                     help="--case forest: number of point clouds (trees)")
-    ap.add_argument("--case", default="knn", choices=["knn", "build", "nearest", "radius", "forest", "serve"],
+    ap.add_argument("--kdop", type=int, default=14, choices=[6, 14, 18, 26],
+                    help="--case kdop: KDOP<3, k> of the values")
+    ap.add_argument("--case", default="knn",
+                    choices=["knn", "build", "nearest", "radius", "forest", "serve", "kdop"],
                     help="knn: the benchmark step (build + kNN); build / nearest / radius: "
                     "one stage alone (profiling cases; radius = 2-pass CRS search with "
                     "~32 expected neighbours)")
@@ -579,6 +582,68 @@ def run_case(args):
     }), flush=True)
 
 
+def make_segments(n, seed=21):
+    """n line segments: a uniform start point in [0,1)^3 and a random
+    direction of length 4 / n^(1/3) (four mean point spacings), as float32
+    endpoints [n, 3] each."""
+    rng = np.random.default_rng(seed)
+    a = rng.random((n, 3), dtype=np.float32)
+    d = rng.standard_normal((n, 3)).astype(np.float32)
+    d *= np.float32(4.0 / n ** (1 / 3)) / np.linalg.norm(d, axis=1, keepdims=True).astype(np.float32)
+    return a, a + d
+
+
+def run_kdop(args):
+    """KDOP-bounded tree over n slanted segments (KDOP<3, k> of the two
+    endpoints) against the box tree of the same segments' axis boxes: build
+    time, and nq box queries of edge 1 / n^(1/3) through each (hits differ:
+    the KDOP tree tests the tighter KDOPs)."""
+    import torch
+
+    import arborx_gb300 as ax
+    from arborx_gb300 import build as libbuild
+
+    libbuild.build()
+    n, nq, k = args.n, args.nq, args.kdop
+    a, b = make_segments(n)
+    ka = ax.kdop_from(torch.from_numpy(a).cuda(), k)
+    kb = ax.kdop_from(torch.from_numpy(b).cuda(), k)
+    nd = k // 2
+    kd = torch.cat([torch.minimum(ka[:, :nd], kb[:, :nd]), torch.maximum(ka[:, nd:], kb[:, nd:])], 1)
+    del ka, kb
+    boxes = torch.cat([kd[:, 0:3], kd[:, nd:nd + 3]], 1).contiguous()
+    kind = {6: ax.KDOP6, 14: ax.KDOP14, 18: ax.KDOP18, 26: ax.KDOP26}[k]
+    c = np.random.default_rng(22).random((nq, 3), dtype=np.float32)
+    h = np.float32(0.5 / n ** (1 / 3))
+    qb = torch.from_numpy(np.concatenate([c - h, c + h], 1)).cuda()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            keep = fn()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            keep = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps, keep
+
+    ms_kbuild, ktree = timed(lambda: ax.BVH(kd, kind=kind))
+    ms_bbuild, btree = timed(lambda: ax.BVH(boxes))
+    ms_kq, (kidx, koff) = timed(lambda: ax.query(ktree, ax.intersects(qb)))
+    ms_bq, (bidx, boff) = timed(lambda: ax.query(btree, ax.intersects(qb)))
+    print(json.dumps({
+        "case": "kdop", "k": k, "n": n, "nq": nq, "values": "segments, length 4 n^(-1/3)",
+        "build_ms": {"kdop": ms_kbuild, "box": ms_bbuild},
+        "query_ms": {"kdop": ms_kq, "box": ms_bq},
+        "queries_per_s": {"kdop": nq / (ms_kq * 1e-3), "box": nq / (ms_bq * 1e-3)},
+        "hits_per_query": {"kdop": int(koff[-1]) / nq, "box": int(boff[-1]) / nq},
+        "kdop_node_bytes": (2 * max(n - 1, 1) + 1) * 4 * ((2 * nd + 3) // 4) * 4,
+    }), flush=True)
+
+
 def make_clouds(ncl):
     """The batched workload: ncl clouds of floor(10^U(2,5)) points (seed 13);
     cloud i has its lower corner in U[0,100)^3 and extents 10^U(-1,1) per axis
@@ -778,6 +843,8 @@ def main():
         run_forest(args)
     elif args.case == "serve":
         run_serve(args)
+    elif args.case == "kdop":
+        run_kdop(args)
     elif args.case != "knn":
         run_case(args)
     else:
