@@ -98,7 +98,90 @@ struct Ray
   Point direction;
   __host__ __device__ Point const &origin_point() const { return origin; }
 };
+
+// ArborX::Experimental::KDOP<3, k> (src/geometry/ArborX_KDOP.hpp:155-183),
+// k = 6, 14, 18, 26: the ranges of the k/2 directions, min then max, as in
+// the reference's struct and the C ABI rows.  Default: every range empty.
+template <int DIM, int k, class Coordinate = float>
+struct KDOP
+{
+  static_assert(DIM == 3 && std::is_same_v<Coordinate, float> &&
+                    (k == 6 || k == 14 || k == 18 || k == 26),
+                "KDOP<3, 6 | 14 | 18 | 26, float>");
+  static constexpr int n_directions = k / 2;
+  float _min_values[k / 2];
+  float _max_values[k / 2];
+  KDOP()
+  {
+    for (int i = 0; i < n_directions; ++i)
+    {
+      _min_values[i] = 3.40282347e38f;
+      _max_values[i] = -3.40282347e38f;
+    }
+  }
+};
 } // namespace Experimental
+
+namespace Details
+{
+// Direction i of KDOP<3, 2 n> (ArborX_KDOP.hpp:64-151): the axes, then the
+// edges (k = 18, 26), then the corners (k = 14, 26).
+inline void kdop_direction(int n, int i, float d[3])
+{
+  static const float edges[6][3] = {{1, 1, 0}, {1, 0, 1}, {0, 1, 1},
+                                    {1, -1, 0}, {1, 0, -1}, {0, 1, -1}};
+  static const float corners[4][3] = {{1, 1, 1}, {1, -1, 1}, {1, 1, -1}, {1, -1, -1}};
+  const float *v = nullptr;
+  float axis[3] = {0, 0, 0};
+  if (i < 3)
+  {
+    axis[i] = 1;
+    v = axis;
+  }
+  else if (n == 7)
+    v = corners[i - 3];
+  else if (i < 9)
+    v = edges[i - 3];
+  else
+    v = corners[i - 9];
+  d[0] = v[0];
+  d[1] = v[1];
+  d[2] = v[2];
+}
+} // namespace Details
+
+// expand(KDOP, Point) and expand(KDOP, Box) on the host
+// (algorithms/ArborX_Expand.hpp:128-208): the same projections (one rounding
+// per operation; compile without FMA contraction to match bit for bit) and
+// Kokkos::min/max.
+template <int k>
+void expand(Experimental::KDOP<3, k> &x, Point const &p)
+{
+  for (int i = 0; i < k / 2; ++i)
+  {
+    float d[3];
+    Details::kdop_direction(k / 2, i, d);
+    float proj = p[0] * d[0];
+    proj += p[1] * d[1];
+    proj += p[2] * d[2];
+    x._min_values[i] = proj < x._min_values[i] ? proj : x._min_values[i];
+    x._max_values[i] = x._max_values[i] < proj ? proj : x._max_values[i];
+  }
+}
+template <int k>
+void expand(Experimental::KDOP<3, k> &x, Box const &b)
+{
+  for (int d = 0; d < 3; ++d)
+    if (b.minCorner()[d] > b.maxCorner()[d])
+      return;
+  for (int c = 0; c < 8; ++c)
+  {
+    Point const &px = (c >> 2) & 1 ? b.maxCorner() : b.minCorner();
+    Point const &py = c & 1 ? b.maxCorner() : b.minCorner();
+    Point const &pz = (c >> 1) & 1 ? b.maxCorner() : b.minCorner();
+    expand(x, Point{{px[0], py[1], pz[2]}});
+  }
+}
 
 static_assert(sizeof(Point) == 12 && sizeof(Box) == 24 && sizeof(Sphere) == 16 &&
                   sizeof(Experimental::Ray) == 24,
@@ -185,6 +268,18 @@ inline abx_traversal_policy c_policy(Policy const &p)
   return abx_traversal_policy{p._buffer_size, p._sort_predicates ? 1 : 0};
 }
 
+template <class T>
+struct kdop_kind
+{
+  static constexpr abx_geometry value = ABX_POINT; // not a KDOP
+};
+template <int k>
+struct kdop_kind<Experimental::KDOP<3, k>>
+{
+  static constexpr abx_geometry value =
+      k == 6 ? ABX_KDOP6 : k == 14 ? ABX_KDOP14 : k == 18 ? ABX_KDOP18 : ABX_KDOP26;
+};
+
 template <class Geometry>
 constexpr abx_geometry predicate_kind()
 {
@@ -192,6 +287,8 @@ constexpr abx_geometry predicate_kind()
     return ABX_SPHERE;
   else if constexpr (std::is_same_v<Geometry, Box>)
     return ABX_BOX;
+  else if constexpr (kdop_kind<Geometry>::value != ABX_POINT)
+    return kdop_kind<Geometry>::value;
   else
     return ABX_RAY;
 }
@@ -222,8 +319,9 @@ template <class Geometry>
 struct Intersects
 {
   static_assert(std::is_same_v<Geometry, Sphere> || std::is_same_v<Geometry, Box> ||
-                    std::is_same_v<Geometry, Experimental::Ray>,
-                "intersects predicates are spheres, boxes or rays");
+                    std::is_same_v<Geometry, Experimental::Ray> ||
+                    Details::kdop_kind<Geometry>::value != ABX_POINT,
+                "intersects predicates are spheres, boxes, rays or KDOPs");
   DeviceView<Geometry> geometries;
 };
 
@@ -293,6 +391,15 @@ public:
   BoundingVolumeHierarchy(cudaStream_t space, DeviceView<Box> const &boxes)
   {
     create(space, ABX_BOX, reinterpret_cast<const float *>(boxes.data()), (int64_t)boxes.size());
+  }
+  // BVH<MemorySpace, PairValueIndex<KDOP>, DefaultIndexableGetter, KDOP>: KDOP
+  // values, nodes bounded by KDOPs of the same directions
+  // (ArborX_LinearBVH.hpp:56-60; test/CMakeLists.txt:126-151)
+  template <int k>
+  BoundingVolumeHierarchy(cudaStream_t space, DeviceView<Experimental::KDOP<3, k>> const &kdops)
+  {
+    create(space, Details::kdop_kind<Experimental::KDOP<3, k>>::value,
+           reinterpret_cast<const float *>(kdops.data()), (int64_t)kdops.size());
   }
 
   size_type size() const noexcept { return abx_bvh_size(_tree.get()); }

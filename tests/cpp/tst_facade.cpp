@@ -316,6 +316,38 @@ static void ordered_rays()
   CHECK((ind.to_host() == std::vector<int>{0, 9}));
 }
 
+// test/tstQueryTreeIntersectsKDOP.cpp:26-91: a KDOP<3, 18> (a box with an
+// edge cut off) over 13 points; then the same points as KDOP<3, 18> values
+// in a KDOP-bounded tree.
+static void intersects_kdop()
+{
+  std::vector<Point> prims = {{{0, 0, 0}}, {{1, 1, 1}}, {{2, 2, 2}}, {{3, 3, 3}}, {{1, 0, 0}},
+                              {{2, 0, 0}}, {{3, 0, 0}}, {{0, 1, 0}}, {{0, 2, 0}}, {{0, 3, 0}},
+                              {{0, 0, 1}}, {{0, 0, 2}}, {{0, 0, 3}}};
+  BVH tree(nullptr, DeviceView<Point>(prims));
+  using K18 = Experimental::KDOP<3, 18>;
+  K18 x;
+  for (Point p : std::vector<Point>{{{0.25f, 0, 0}}, {{1, 0, 0}}, {{1, 2, 0}}, {{0, 2, 0}},
+                                    {{0, 0.25f, 0}}, {{0.25f, 0, 3}}, {{1, 0, 3}}, {{1, 2, 3}},
+                                    {{0, 2, 3}}, {{0, 0.25f, 3}}})
+    expand(x, p);
+  DeviceView<K18> preds(std::vector<K18>{x});
+  DeviceView<int> ind, off;
+  tree.query(nullptr, intersects(preds), ind, off);
+  CHECK(same_crs({off.to_host(), ind.to_host()}, {0, 4}, {1, 4, 7, 8}));
+  tree.query(nullptr, intersects(DeviceView<K18>()), ind, off);
+  CHECK((off.to_host() == std::vector<int>{0}));
+  std::vector<K18> values(prims.size());
+  for (size_t i = 0; i < prims.size(); ++i)
+    expand(values[i], prims[i]);
+  BVH ktree(nullptr, DeviceView<K18>(values));
+  ktree.query(nullptr, intersects(preds), ind, off);
+  CHECK(same_crs({off.to_host(), ind.to_host()}, {0, 4}, {1, 4, 7, 8}));
+  DeviceView<Box> unit(std::vector<Box>{Box(Point{{0, 0, 0}}, Point{{1, 1, 1}})});
+  ktree.query(nullptr, intersects(unit), ind, off);
+  CHECK(same_crs({off.to_host(), ind.to_host()}, {0, 5}, {0, 1, 4, 7, 10}));
+}
+
 int main()
 {
   empty_tree();
@@ -330,6 +362,7 @@ int main()
   brute_force_matches_tree();
   neighbor_lists();
   ordered_rays();
+  intersects_kdop();
   std::printf("%d checks, %d failures\n", g_checks, g_failures);
   return g_failures == 0 ? 0 : 1;
 }
