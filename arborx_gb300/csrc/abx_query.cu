@@ -175,9 +175,9 @@ __device__ __forceinline__ KnnTask knn_task(int64_t t, int64_t n, ForestView con
 
 // One query per thread.  The list keeps K slots; the first K - k hold the
 // key 0 (never displaced), so the k-th best is always slot K - 1.  thr is
-// sq_threshold of the k-th best distance (+inf until the list is full): a
-// node or leaf whose squared distance s satisfies s <= thr can still hold a
-// better candidate.  Buckets are scanned as soon as their box passes; of two
+// sq_bound of the k-th best distance (+inf until the list is full): a node
+// or leaf whose squared distance s satisfies s <= thr may hold a better
+// candidate (and every one that can passes).  Buckets are scanned as soon as their box passes; of two
 // passing internal children the closer is visited first and the other waits
 // on the stack with its squared distance.
 // Up to 16 keys the register list fits in 64 registers per thread, which
@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(kQueryThreads, K <= 16 ? 8 : 1)
     {
       list_insert<K>(key, c);
       if (key[K - 1] != kKeyEmpty)
-        thr = sq_threshold(key_dist(key[K - 1]));
+        thr = sq_bound(key_dist(key[K - 1]));
     }
   };
   // s_box: squared distance to the bucket's box (for a single leaf, its

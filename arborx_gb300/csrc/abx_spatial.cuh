@@ -75,6 +75,18 @@ __device__ __forceinline__ float sq_threshold(float r)
   return t;
 }
 
+// A bound above sq_threshold(r) within a few ulps, without square roots.
+// sqrt_rn(s) <= r needs sqrt(s) <= r + ulp(r)/2, i.e. s <= r^2 + r ulp(r) +
+// ulp(r)^2/4, and r ulp(r) <= 2 ulp(r^2): RU(r r) + 3 ulps lies above every
+// such s (subnormal squares included).  Pruning with it visits a few more
+// candidates than the exact threshold and keeps every result exact, because
+// a candidate enters the k-nearest list only by its exact key.
+__device__ __forceinline__ float sq_bound(float r)
+{
+  const float t = __fmul_ru(r, r);
+  return t < INFINITY ? __uint_as_float(__float_as_uint(t) + 3u) : INFINITY;
+}
+
 // Squared distance from a point to a leaf's bounding volume.
 template <int KIND>
 __device__ __forceinline__ float leaf_dist2(float qx, float qy, float qz, Box3 const &b)
