@@ -37,6 +37,7 @@ from .bvh import (  # noqa: F401
     ordered_intersects,
     ray_intersects,
     query,
+    query_nearest_host,
     query_nearest_into,
     scene_bounds,
     sort_u32,

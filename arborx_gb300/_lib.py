@@ -133,6 +133,8 @@ SIGNATURES = {
     "abx_bvh_query_ordered_intersects": (
         _STATUS, [_P, _P, _P, _I64, _I32, TraversalPolicyC, _I32, ctypes.POINTER(_P)],
     ),
+    "abx_bvh_query_nearest_host": (_STATUS, [_P, _P, _P, _I64, ctypes.c_int32, TraversalPolicyC, _I64,
+                                             _P, _P, _P]),
     "abx_bvh_query_nearest_into": (
         _STATUS, [_P, _P, _P, _I64, _I32, TraversalPolicyC, _P, _P, _P],
     ),

@@ -394,6 +394,31 @@ def query_nearest_into(tree, queries, k, offsets, indices, distances=None, polic
         _ptr(indices), _ptr(distances) if distances is not None else None))
 
 
+def query_nearest_host(tree, queries, k, offsets, indices, distances=None, chunk=0, policy=None,
+                       space=None):
+    """nearest(point, k) with the queries [nq, 3] and the results in host
+    memory (float32 / int32 CPU tensors; pinned for the copies to overlap):
+    offsets [nq + 1], indices [nq * min(k, size)], distances optional.  The
+    queries move to the device in chunks pipelined with the traversal and the
+    copies back (abx_bvh_query_nearest_host)."""
+    policy = policy or TraversalPolicy()
+    for t, name, dt in ((queries, "queries", torch.float32), (offsets, "offsets", torch.int32),
+                        (indices, "indices", torch.int32)):
+        if not (isinstance(t, torch.Tensor) and not t.is_cuda and t.dtype == dt and t.is_contiguous()):
+            raise TypeError("%s must be a contiguous %s CPU tensor" % (name, dt))
+    if distances is not None and not (isinstance(distances, torch.Tensor) and not distances.is_cuda
+                                      and distances.dtype == torch.float32 and distances.is_contiguous()):
+        raise TypeError("distances must be a contiguous float32 CPU tensor")
+    nq = queries.shape[0] if queries.dim() == 2 else queries.numel() // 3
+    kk = min(max(int(k), 0), tree.size())
+    if offsets.numel() < nq + 1 or indices.numel() < nq * kk or (
+            distances is not None and distances.numel() < nq * kk):
+        raise ValueError("query_nearest_host: output tensors too small")
+    check(_lib.load().abx_bvh_query_nearest_host(
+        tree._h, _stream(space), queries.data_ptr(), nq, int(k), policy._c(), int(chunk),
+        offsets.data_ptr(), indices.data_ptr(), distances.data_ptr() if distances is not None else None))
+
+
 def _neighbor_list(points, radius, half, space):
     p = _as_rows(points, 3, "points")
     h = ctypes.c_void_p()

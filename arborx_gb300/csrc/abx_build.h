@@ -203,6 +203,10 @@ abx_status launch_nearest(cudaStream_t s, TreeView const &t, ForestView const *f
                           const int32_t *d_k, int32_t k, int32_t max_k, const int32_t *d_offsets,
                           int32_t *d_offsets_out, int32_t *d_idx, float *d_dist);
 
+// d_out[i] = (first + i) * step for i < count (CRS offsets of a fixed k).
+abx_status fill_offsets_iota(cudaStream_t s, int32_t *d_out, int64_t count, int64_t first,
+                             int64_t step);
+
 // counts[q] = min(max(k_q, 0), size of q's tree) with k_q = d_k[q] (or k
 // when d_k is null); max of k_q over queries into *d_max (zeroed).
 abx_status launch_knn_counts(cudaStream_t s, TreeView const &t, ForestView const *f,

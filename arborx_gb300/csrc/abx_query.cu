@@ -925,6 +925,26 @@ abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int3
   return ABX_SUCCESS;
 }
 
+namespace
+{
+__global__ void k_offsets_iota(int32_t *__restrict__ out, int64_t count, int64_t first, int64_t step)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count)
+    out[i] = (int32_t)((first + i) * step);
+}
+} // namespace
+
+abx_status fill_offsets_iota(cudaStream_t s, int32_t *d_out, int64_t count, int64_t first,
+                             int64_t step)
+{
+  if (count <= 0)
+    return ABX_SUCCESS;
+  k_offsets_iota<<<(unsigned)((count + 255) / 256), 256, 0, s>>>(d_out, count, first, step);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
+
 abx_status launch_nearest(cudaStream_t s, TreeView const &t, ForestView const *fp,
                           const float *d_queries, int64_t nq, const uint32_t *d_perm,
                           const int32_t *d_k, int32_t k, int32_t max_k, const int32_t *d_offsets,

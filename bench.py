@@ -409,13 +409,13 @@ def run_gpu(args):
     out_off_h = torch.empty(args.nq + 1, dtype=torch.int32).pin_memory()
 
     def e2e_step():
+        # the build from the host points, then the kNN call with host
+        # queries and host results (chunked, copies pipelined with the
+        # traversal); the call returns with the results on the host
         p = points_h.to("cuda", non_blocking=True)
-        q = queries_h.to("cuda", non_blocking=True)
         bvh = ax.BoundingVolumeHierarchy(p)
-        ind, off = ax.query(bvh, ax.nearest(q, args.k))
-        out_idx_h.copy_(ind, non_blocking=True)
-        out_off_h.copy_(off, non_blocking=True)
-        return bvh, ind, off, p, q
+        ax.query_nearest_host(bvh, queries_h, args.k, out_off_h, out_idx_h)
+        return bvh, p
 
     for _ in range(2):
         keep = e2e_step()

@@ -464,6 +464,24 @@ ABX_API abx_status abx_bvh_query_nearest_into(const abx_bvh *bvh, void *stream,
                                               abx_traversal_policy policy, int32_t *d_offsets,
                                               int32_t *d_indices, float *d_distances);
 
+/* nearest(point, k) with the queries and the results in HOST memory: the
+ * call a host-side plugin makes (the reference's query(space, predicates,
+ * indices, offsets) with host Views).  The queries go to the device in
+ * chunks of `chunk` queries (<= 0: 40% of them, at least 2^18) over two
+ * copy streams, so that
+ * chunk i + 1 moves in and the results of chunk i - 1 move out while chunk i
+ * is traversed; each chunk is ordered by Morton code by itself when
+ * policy.sort_predicates is set.  h_offsets (nq + 1), h_indices
+ * (nq * min(k, size())) and, if not NULL, h_distances receive exactly what
+ * abx_bvh_query_nearest returns.  Host buffers should be pinned
+ * (cudaHostAlloc or cudaHostRegister) for the copies to overlap.  Returns
+ * when the results are on the host. */
+ABX_API abx_status abx_bvh_query_nearest_host(const abx_bvh *bvh, void *stream,
+                                              const float *h_queries, int64_t nq, int32_t k,
+                                              abx_traversal_policy policy, int64_t chunk,
+                                              int32_t *h_offsets, int32_t *h_indices,
+                                              float *h_distances);
+
 /* Accessors of a CRS result: device offsets (nq + 1), device indices
  * (num_results), device distances (nearest only, else NULL). */
 ABX_API int64_t abx_crs_num_queries(const abx_crs *crs);
