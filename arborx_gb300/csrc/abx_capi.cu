@@ -1125,6 +1125,20 @@ abx_status abx_bvh_query_nearest(const abx_bvh *bvh, void *stream, const float *
 
 namespace abx
 {
+// Device address of page-locked host memory mapped into the device's address
+// space (cudaHostAlloc / cudaHostRegister on a unified-address system); null
+// for any other pointer.
+void *mapped_host_pointer(void *h)
+{
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess)
+  {
+    cudaGetLastError(); // clear the error of an unknown pointer
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 // Smallest chunk of the default schedule of abx_bvh_query_nearest_host.
 constexpr int64_t kHostMinChunk = (int64_t)1 << 18;
 
@@ -1220,6 +1234,23 @@ abx_status abx_bvh_query_nearest_host(const abx_bvh *bvh, void *stream, const fl
     return ABX_SUCCESS;
   }
   ABX_CUDA_TRY(cudaStreamWaitEvent(s, bvh->ready, 0));
+  // Pinned (page-locked, device-mapped) result buffers are written by the
+  // traversal itself over the CPU-GPU link: no result copy after the last
+  // query, no chunking.  Other host memory takes the chunked copies below.
+  void *dev_off = mapped_host_pointer(h_offsets), *dev_idx = mapped_host_pointer(h_indices);
+  void *dev_dist = h_distances ? mapped_host_pointer(h_distances) : nullptr;
+  if (chunk <= 0 && dev_off && dev_idx && (!h_distances || dev_dist) &&
+      tuning_value("HOST_DIRECT", 1))
+  {
+    Scratch<float> dq;
+    ABX_CUDA_TRY(dq.alloc((size_t)nq * 3, s));
+    ABX_CUDA_TRY(cudaMemcpyAsync(dq.ptr, h_queries, (size_t)nq * 3 * sizeof(float),
+                                 cudaMemcpyHostToDevice, s));
+    ABX_TRY(nearest_into(bvh, s, dq.ptr, nq, k, policy, false, nullptr,
+                         static_cast<int32_t *>(dev_idx), static_cast<float *>(dev_dist)));
+    ABX_TRY(fill_offsets_iota(s, static_cast<int32_t *>(dev_off), nq + 1, 0, kk));
+    return sync_and_check(s);
+  }
   // chunk boundaries: a fixed size, by default 40% of the queries (at least
   // kHostMinChunk): the traversal of a chunk gets slower as its Morton-sorted
   // queries thin out in space (1e7 uniform queries, k = 16: chunks of 40%

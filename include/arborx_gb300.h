@@ -471,11 +471,13 @@ ABX_API abx_status abx_bvh_query_nearest_into(const abx_bvh *bvh, void *stream,
  * copy streams, so that
  * chunk i + 1 moves in and the results of chunk i - 1 move out while chunk i
  * is traversed; each chunk is ordered by Morton code by itself when
- * policy.sort_predicates is set.  h_offsets (nq + 1), h_indices
- * (nq * min(k, size())) and, if not NULL, h_distances receive exactly what
- * abx_bvh_query_nearest returns.  Host buffers should be pinned
- * (cudaHostAlloc or cudaHostRegister) for the copies to overlap.  Returns
- * when the results are on the host. */
+ * policy.sort_predicates is set.  When chunk <= 0 and the result buffers
+ * are page-locked and mapped (cudaHostAlloc, cudaHostRegister: every pinned
+ * buffer on a unified-address system), there are no chunks: the traversal
+ * writes the results straight into them over the CPU-GPU link.  h_offsets
+ * (nq + 1), h_indices (nq * min(k, size())) and, if not NULL, h_distances
+ * receive exactly what abx_bvh_query_nearest returns.  Returns when the
+ * results are on the host. */
 ABX_API abx_status abx_bvh_query_nearest_host(const abx_bvh *bvh, void *stream,
                                               const float *h_queries, int64_t nq, int32_t k,
                                               abx_traversal_policy policy, int64_t chunk,
