@@ -78,6 +78,7 @@ SIGNATURES = {
     "abx_profiling_reset": (_STATUS, []),
     "abx_bvh_create": (_STATUS, [_P, ctypes.c_int, _P, _I64, ctypes.POINTER(_P)]),
     "abx_bvh_create_strided": (_STATUS, [_P, ctypes.c_int, ValuesC, _I64, ctypes.POINTER(_P)]),
+    "abx_gather_rows": (_STATUS, [_P, _P, _I64, _I64, _P, _I64, _P]),
     "abx_kdop_from_geometry": (_STATUS, [_P, ctypes.c_int, _P, _I64, ctypes.c_int, _P]),
     "abx_bvh_kdop_bounds": (_STATUS, [_P, _P]),
     "abx_bvh_save": (_STATUS, [_P, ctypes.c_char_p]),

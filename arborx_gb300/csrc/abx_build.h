@@ -203,6 +203,11 @@ abx_status launch_nearest(cudaStream_t s, TreeView const &t, ForestView const *f
                           const int32_t *d_k, int32_t k, int32_t max_k, const int32_t *d_offsets,
                           int32_t *d_offsets_out, int32_t *d_idx, float *d_dist);
 
+// d_dst row j = d_src row d_rows[j] (rows of `words` 32-bit words; rows
+// outside [0, n_src) raise the device error word and give zeros).
+abx_status gather_rows(cudaStream_t s, const void *d_src, int64_t n_src, int words,
+                       const int32_t *d_rows, int64_t m, void *d_dst);
+
 // d_out[i] = (first + i) * step for i < count (CRS offsets of a fixed k).
 abx_status fill_offsets_iota(cudaStream_t s, int32_t *d_out, int64_t count, int64_t first,
                              int64_t step);

@@ -1018,6 +1018,16 @@ abx_status abx_bvh_kdop_bounds(const abx_bvh *bvh, float *h_kdop)
   return ABX_SUCCESS;
 }
 
+abx_status abx_gather_rows(void *stream, const void *d_src, int64_t n_src, int64_t row_bytes,
+                           const int32_t *d_rows, int64_t m, void *d_dst)
+{
+  if (row_bytes <= 0 || row_bytes % 4 != 0 || row_bytes > ((int64_t)1 << 20) || n_src < 0 ||
+      m < 0 || (m > 0 && (!d_src || !d_rows || !d_dst)))
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "abx_gather_rows: bad arguments");
+  device_state();
+  return gather_rows(as_stream(stream), d_src, n_src, (int)(row_bytes / 4), d_rows, m, d_dst);
+}
+
 abx_status abx_kdop_from_geometry(void *stream, abx_geometry kind, const float *d_values,
                                   int64_t n, abx_geometry kdop_kind, float *d_kdops)
 {

@@ -927,6 +927,27 @@ abx_status launch_compact(cudaStream_t s, const int32_t *d_tmp, int64_t nq, int3
 
 namespace
 {
+// dst row j = src row rows[j], rows of w 32-bit words (a value gather of the
+// query results).
+__global__ void k_gather_rows(const uint32_t *__restrict__ src, int64_t n_src, int w,
+                              const int32_t *__restrict__ rows, int64_t m,
+                              uint32_t *__restrict__ dst, unsigned *__restrict__ err)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m * w)
+    return;
+  const int64_t j = i / w;
+  const int c = (int)(i - j * w);
+  const int32_t r = __ldg(rows + j);
+  if ((uint64_t)r >= (uint64_t)n_src)
+  {
+    raise_error(err, ABX_DEVERR_INTERNAL);
+    dst[i] = 0;
+    return;
+  }
+  dst[i] = __ldg(src + (int64_t)r * w + c);
+}
+
 __global__ void k_offsets_iota(int32_t *__restrict__ out, int64_t count, int64_t first, int64_t step)
 {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -934,6 +955,19 @@ __global__ void k_offsets_iota(int32_t *__restrict__ out, int64_t count, int64_t
     out[i] = (int32_t)((first + i) * step);
 }
 } // namespace
+
+abx_status gather_rows(cudaStream_t s, const void *d_src, int64_t n_src, int words,
+                       const int32_t *d_rows, int64_t m, void *d_dst)
+{
+  if (m <= 0)
+    return ABX_SUCCESS;
+  const int64_t total = m * words;
+  k_gather_rows<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(
+      static_cast<const uint32_t *>(d_src), n_src, words, d_rows, m, static_cast<uint32_t *>(d_dst),
+      device_state().d_error);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
+}
 
 abx_status fill_offsets_iota(cudaStream_t s, int32_t *d_out, int64_t count, int64_t first,
                              int64_t step)

@@ -164,6 +164,15 @@ typedef struct abx_values
 ABX_API abx_status abx_bvh_create_strided(void *stream, abx_geometry kind, abx_values values,
                                           int64_t n, abx_bvh **out);
 
+/* Values of query results (PairValueIndex values, ArborX_PairValueIndex.hpp:
+ * 23-44, or any record the caller stores per value): d_dst row j = d_src row
+ * d_rows[j] for j < m, rows of row_bytes bytes (a multiple of 4); d_src holds
+ * n_src rows (device memory).  An index outside [0, n_src) sets the device
+ * error word and gives a zero row.  Asynchronous on `stream`. */
+ABX_API abx_status abx_gather_rows(void *stream, const void *d_src, int64_t n_src,
+                                   int64_t row_bytes, const int32_t *d_rows, int64_t m,
+                                   void *d_dst);
+
 /* KDOP bounding volumes (src/geometry/ArborX_KDOP.hpp; the BoundingVolume
  * parameter of BoundingVolumeHierarchy, src/spatial/ArborX_LinearBVH.hpp:
  * 56-60).  abx_bvh_create with kind ABX_KDOP6/14/18/26 builds a tree over n

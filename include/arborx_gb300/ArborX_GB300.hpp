@@ -183,6 +183,29 @@ void expand(Experimental::KDOP<3, k> &x, Box const &b)
   }
 }
 
+// ArborX::PairValueIndex (src/spatial/detail/ArborX_PairValueIndex.hpp:
+// 23-44): a value stored with the caller's index; a tree over them indexes
+// their geometry and returns the pairs themselves.
+template <class Value, class Index = int>
+struct PairValueIndex
+{
+  static_assert(std::is_same_v<Value, Point> || std::is_same_v<Value, Box>,
+                "PairValueIndex of points or boxes");
+  static_assert(std::is_same_v<Index, int> || std::is_same_v<Index, unsigned>,
+                "32-bit indices");
+  Value value;
+  Index index;
+};
+
+template <class T>
+struct is_pair_value_index : std::false_type
+{
+};
+template <class V, class I>
+struct is_pair_value_index<PairValueIndex<V, I>> : std::true_type
+{
+};
+
 static_assert(sizeof(Point) == 12 && sizeof(Box) == 24 && sizeof(Sphere) == 16 &&
                   sizeof(Experimental::Ray) == 24,
               "geometry rows must match the C ABI");
@@ -402,6 +425,26 @@ public:
            reinterpret_cast<const float *>(kdops.data()), (int64_t)kdops.size());
   }
 
+  // BVH<MemorySpace, PairValueIndex<Point | Box>>: the tree indexes the
+  // pairs' geometry (read through their stride, ArborX_AccessTraits.hpp:
+  // 36-76) and keeps a copy of the pairs, which value queries return.
+  template <class V, class I>
+  BoundingVolumeHierarchy(cudaStream_t space, DeviceView<PairValueIndex<V, I>> const &values)
+  {
+    using P = PairValueIndex<V, I>;
+    static_assert(sizeof(P) % 4 == 0, "pairs of 32-bit words");
+    const abx_geometry kind = std::is_same_v<V, Point> ? ABX_POINT : ABX_BOX;
+    abx_values strided{reinterpret_cast<const float *>(values.data()), (int64_t)(sizeof(P) / 4), 1};
+    abx_bvh *t = nullptr;
+    Details::check(abx_bvh_create_strided(space, kind, strided, (int64_t)values.size(), &t));
+    _tree.reset(t, [](abx_bvh *p) { abx_bvh_destroy(p); });
+    _values.realloc(values.size() * sizeof(P) / 4);
+    if (values.size())
+      Details::check_cuda(cudaMemcpyAsync(_values.data(), values.data(), values.size() * sizeof(P),
+                                          cudaMemcpyDeviceToDevice, space));
+    _value_bytes = sizeof(P);
+  }
+
   size_type size() const noexcept { return abx_bvh_size(_tree.get()); }
   bool empty() const noexcept { return size() == 0; }
   Box bounds() const
@@ -409,6 +452,23 @@ public:
     float b[6];
     Details::check(abx_bvh_bounds(_tree.get(), b));
     return Box(Point{{b[0], b[1], b[2]}}, Point{{b[3], b[4], b[5]}});
+  }
+
+  // query(space, predicates, values, offsets[, policy]) on a tree of pairs:
+  // the matching pairs themselves in the CRS order of the indices.
+  template <class Predicates, class V, class I>
+  void query(cudaStream_t space, Predicates const &preds, DeviceView<PairValueIndex<V, I>> &values,
+             DeviceView<int> &offsets,
+             Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy()) const
+  {
+    using P = PairValueIndex<V, I>;
+    if (_value_bytes != sizeof(P))
+      throw SearchException("query: the tree was not built from these PairValueIndex values");
+    DeviceView<int> indices;
+    query(space, preds, indices, offsets, policy);
+    values.realloc(indices.size());
+    Details::check(abx_gather_rows(space, _values.data(), size(), (int64_t)sizeof(P),
+                                   indices.data(), (int64_t)indices.size(), values.data()));
   }
 
   // query(space, predicates, indices, offsets[, policy]): the callee
@@ -466,6 +526,8 @@ private:
     return Details::c_policy(p);
   }
   std::shared_ptr<abx_bvh> _tree;
+  DeviceView<float> _values; // the pairs of a PairValueIndex tree
+  size_t _value_bytes = 0;
 };
 
 using BVH = BoundingVolumeHierarchy;

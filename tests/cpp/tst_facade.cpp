@@ -348,6 +348,35 @@ static void intersects_kdop()
   CHECK(same_crs({off.to_host(), ind.to_host()}, {0, 5}, {0, 1, 4, 7, 10}));
 }
 
+// PairValueIndex values (ArborX_PairValueIndex.hpp:23-44; the test suite's
+// trees, test/ArborXTest_LegacyTree.hpp:38-60): queries return the pairs.
+static void pair_value_index()
+{
+  std::vector<PairValueIndex<Point>> pairs;
+  for (int i = 0; i < 10; ++i)
+    pairs.push_back({Point{{(float)i, (float)i, (float)i}}, 100 + i});
+  BVH tree(nullptr, DeviceView<PairValueIndex<Point>>(pairs));
+  DeviceView<Box> q(std::vector<Box>{Box(Point{{2.5f, 2.5f, 2.5f}}, Point{{5, 5, 5}}),
+                                     Box(Point{{-1, -1, -1}}, Point{{0, 0, 0}})});
+  DeviceView<PairValueIndex<Point>> values;
+  DeviceView<int> off;
+  tree.query(nullptr, intersects(q), values, off);
+  CHECK((off.to_host() == std::vector<int>{0, 3, 4}));
+  std::vector<int> idx;
+  for (auto const &v : values.to_host())
+  {
+    idx.push_back(v.index);
+    CHECK(v.value[0] == (float)(v.index - 100));
+  }
+  CHECK((idx == std::vector<int>{103, 104, 105, 100}));
+  DeviceView<Point> pts(std::vector<Point>{{{7.2f, 7.2f, 7.2f}}});
+  tree.query(nullptr, nearest(pts, 2), values, off);
+  idx.clear();
+  for (auto const &v : values.to_host())
+    idx.push_back(v.index);
+  CHECK((idx == std::vector<int>{107, 108}));
+}
+
 int main()
 {
   empty_tree();
@@ -363,6 +392,7 @@ int main()
   neighbor_lists();
   ordered_rays();
   intersects_kdop();
+  pair_value_index();
   std::printf("%d checks, %d failures\n", g_checks, g_failures);
   return g_failures == 0 ? 0 : 1;
 }
