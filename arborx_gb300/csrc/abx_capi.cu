@@ -1252,13 +1252,43 @@ abx_status abx_bvh_query_nearest_host(const abx_bvh *bvh, void *stream, const fl
   if (chunk <= 0 && dev_off && dev_idx && (!h_distances || dev_dist) &&
       tuning_value("HOST_DIRECT", 1))
   {
-    Scratch<float> dq;
-    ABX_CUDA_TRY(dq.alloc((size_t)nq * 3, s));
+    // the queries move in on their own stream, alongside whatever the tree's
+    // build still runs on s
+    struct Copy
+    {
+      cudaStream_t st = nullptr;
+      cudaEvent_t in = nullptr, done = nullptr;
+      ~Copy()
+      {
+        if (in)
+          cudaEventDestroy(in);
+        if (done)
+          cudaEventDestroy(done);
+        if (st)
+          cudaStreamDestroy(st);
+      }
+    } c;
+    ABX_CUDA_TRY(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
+    ABX_CUDA_TRY(cudaEventCreateWithFlags(&c.in, cudaEventDisableTiming));
+    ABX_CUDA_TRY(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
+    Scratch<float> dq; // allocated and released on the copy stream
+    ABX_CUDA_TRY(dq.alloc((size_t)nq * 3, c.st));
     ABX_CUDA_TRY(cudaMemcpyAsync(dq.ptr, h_queries, (size_t)nq * 3 * sizeof(float),
-                                 cudaMemcpyHostToDevice, s));
-    ABX_TRY(nearest_into(bvh, s, dq.ptr, nq, k, policy, false, nullptr,
-                         static_cast<int32_t *>(dev_idx), static_cast<float *>(dev_dist)));
-    ABX_TRY(fill_offsets_iota(s, static_cast<int32_t *>(dev_off), nq + 1, 0, kk));
+                                 cudaMemcpyHostToDevice, c.st));
+    ABX_CUDA_TRY(cudaEventRecord(c.in, c.st));
+    ABX_CUDA_TRY(cudaStreamWaitEvent(s, c.in, 0));
+    abx_status st = nearest_into(bvh, s, dq.ptr, nq, k, policy, false, nullptr,
+                                 static_cast<int32_t *>(dev_idx), static_cast<float *>(dev_dist));
+    if (st == ABX_SUCCESS)
+      st = fill_offsets_iota(s, static_cast<int32_t *>(dev_off), nq + 1, 0, kk);
+    // the copy stream frees the queries after the traversal read them
+    cudaEventRecord(c.done, s);
+    cudaStreamWaitEvent(c.st, c.done, 0);
+    if (st != ABX_SUCCESS)
+    {
+      cudaStreamSynchronize(s);
+      return st;
+    }
     return sync_and_check(s);
   }
   // chunk boundaries: a fixed size, by default 40% of the queries (at least
