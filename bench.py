@@ -6,8 +6,10 @@ uniform in [0,1)^3 and answer 10^7 nearest(point, k=16) queries drawn from
 the same distribution (CRS output, predicate sorting on, the reference's
 default policy).  `value` is whole-job queries/s of that step with inputs
 resident in HBM; `e2e` is the same step through the public API from pinned
-host buffers (host->device copy of points and queries, device->host copy of
-the CRS indices and offsets inside the timed region).
+host buffers inside the timed region: the points copied to the device and
+the tree built, then abx_bvh_query_nearest_host with the queries, CRS offsets
+and indices in pinned host memory (queries copied in on their own stream,
+results written by the traversal straight into the mapped host buffers).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
