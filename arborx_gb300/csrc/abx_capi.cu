@@ -351,6 +351,9 @@ abx_status build_forest(abx_bvh *t, const float *d_values)
 // Query order: Morton32 codes of the predicates in the scene box; in a
 // forest the tree index ranks above the code, the code taken in the tree's
 // own box.
+// Digits of the predicates' Morton32 codes that order the queries.
+constexpr int kQueryOrderDigits = 3;
+
 abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
                            const float *d_preds, int64_t nq, const int64_t *qoff,
                            Scratch<uint32_t> &perm)
@@ -364,6 +367,13 @@ abx_status sort_predicates(cudaStream_t s, const abx_bvh *t, abx_geometry kind,
   ABX_CUDA_TRY(hist.alloc(4 * 256, s));
   ABX_CUDA_TRY(cudaMemsetAsync(hist.ptr, 0, 4 * 256 * sizeof(uint32_t), s));
   ABX_TRY(morton32_codes(s, kind, d_preds, nq, t->d_bounds, codes.ptr, hist.ptr));
+  // the order only schedules the queries: the top three digits of the code
+  // give the traversal the same coherence as a full sort (1e7 uniform
+  // queries: kNN 17.93 ms either way, ordering 0.39 vs 0.49 ms; two digits
+  // cost the traversal 1.3 ms); 0 asks for the full sort
+  const int digits = tuning_value("QUERY_ORDER_DIGITS", kQueryOrderDigits);
+  if (digits >= 1 && digits <= 3)
+    return radix_order_top_u32(s, codes.ptr, perm.ptr, nq, 4, hist.ptr, digits);
   // the hybrid sort reads a count back to the host: not while capturing
   ABX_TRY(radix_sort_u32(s, codes.ptr, perm.ptr, nullptr, nq, 4, hist.ptr,
                          stream_capturing(s) ? 0 : hybrid_top_passes(nq, 4)));
@@ -1168,8 +1178,12 @@ abx_status nearest_into(const abx_bvh *bvh, cudaStream_t s, const float *d_queri
     ABX_CUDA_TRY(hist.alloc(4 * 256, s));
     ABX_CUDA_TRY(cudaMemsetAsync(hist.ptr, 0, 4 * 256 * sizeof(uint32_t), s));
     ABX_TRY(morton32_codes(s, ABX_POINT, d_queries, nq, bvh->d_bounds, codes.ptr, hist.ptr));
-    ABX_TRY(radix_sort_u32(s, codes.ptr, perm.ptr, nullptr, nq, 4, hist.ptr,
-                           plain_sort ? 0 : hybrid_top_passes(nq, 4)));
+    const int digits = tuning_value("QUERY_ORDER_DIGITS", kQueryOrderDigits);
+    if (digits >= 1 && digits <= 3)
+      ABX_TRY(radix_order_top_u32(s, codes.ptr, perm.ptr, nq, 4, hist.ptr, digits));
+    else
+      ABX_TRY(radix_sort_u32(s, codes.ptr, perm.ptr, nullptr, nq, 4, hist.ptr,
+                             plain_sort ? 0 : hybrid_top_passes(nq, 4)));
   }
   const int64_t kk = std::min<int64_t>(k, bvh->n);
   Scratch<float> dist_tmp;

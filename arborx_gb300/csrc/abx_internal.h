@@ -121,6 +121,11 @@ private:
 abx_status radix_sort_u64(cudaStream_t s, uint64_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,
                           const uint32_t *d_hist, int top_passes = 0);
+// Stable order of n u32 keys by their top `top` of num_passes 8-bit digits
+// only (keys equal there keep their input order): d_perm receives the
+// permutation; d_keys is clobbered.  An ordering for coherence, not a sort.
+abx_status radix_order_top_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_perm, int64_t n,
+                               int num_passes, const uint32_t *d_hist, int top);
 abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
                           const uint32_t *d_vals_in, int64_t n, int num_passes,
                           const uint32_t *d_hist, int top_passes = 0);

@@ -767,6 +767,28 @@ abx_status radix_sort_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_vals,
                                    top_passes);
 }
 
+abx_status radix_order_top_u32(cudaStream_t s, uint32_t *d_keys, uint32_t *d_perm, int64_t n,
+                               int num_passes, const uint32_t *d_hist, int top)
+{
+  if (n <= 0)
+    return ABX_SUCCESS;
+  if (top < 1 || top > num_passes || num_passes > 4)
+    return fail(ABX_ERROR_INVALID_ARGUMENT, "radix order: bad number of digits");
+  StageScope scope(s, "sort32", 0);
+  int launches = 0;
+  Scratch<uint32_t> keys_alt, vals_alt;
+  ABX_CUDA_TRY(keys_alt.alloc(n, s));
+  ABX_CUDA_TRY(vals_alt.alloc(n, s));
+  const uint32_t *kin;
+  const uint32_t *vin;
+  ABX_TRY(sort_passes<uint32_t>(s, d_keys, d_perm, nullptr, n, num_passes - top, num_passes,
+                                d_hist, keys_alt.ptr, vals_alt.ptr, &kin, &vin, launches));
+  if (vin != d_perm)
+    ABX_CUDA_TRY(cudaMemcpyAsync(d_perm, vin, n * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s));
+  scope.add_kernels(launches);
+  return ABX_SUCCESS;
+}
+
 int choose_top_passes(const uint32_t *h_hist, int64_t n, int num_passes)
 {
   const int cap = hybrid_top_passes(n, num_passes);
