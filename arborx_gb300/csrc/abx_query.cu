@@ -576,8 +576,232 @@ __global__ void __launch_bounds__(kQueryThreads)
         {
           list_insert<K>(key, c);
           if (key[K - 1] != kKeyEmpty)
-            thr = sq_threshold(key_dist(key[K - 1]));
+            thr = sq_bound(key_dist(key[K - 1]));
         }
+      }
+    }
+  }
+  if (!work)
+    return;
+  const int kk = task.kk;
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+  {
+    const int r = j - first;
+    if (r >= 0 && r < kk)
+    {
+      out_idx[task.base + r] = key_value(key[j]);
+      if (out_dist)
+        out_dist[task.base + r] = key_dist(key[j]);
+    }
+  }
+}
+
+// Nearest over point values with the all-pairs product on tensor cores as a
+// candidate filter (mma.sync m16n8k8 tf32).  A warp owns 32 queries; per
+// group of 8 points it forms, for its two 16-query row blocks,
+//   C'(q, p) = |p|^2 (1 - e) - 2 q.p,   e = 2^-16,
+// from A rows (qx, qy, qz, 1) and B columns (-2px, -2py, -2pz, |p|^2 (1 - e))
+// split into tf32 high and low parts: one product with K = 8 takes
+// [A_hi | A_lo] x [B_hi ; B_hi], a second A_hi x B_lo (the low x low term is
+// dropped).  The product and accumulation errors stay below 2^-18 (|q|^2 +
+// 2 |p|^2), so V = |q|^2 (1 - e) + C' lies below the real squared distance
+// by more than the float formula's own error: V <= the exact squared
+// distance of the tree's formula.  A pair whose V exceeds the query's
+// pruning bound thr cannot enter its list; every other pair is a candidate,
+// queued per query in shared memory and rescored by the owner lane with the
+// exact formula and key rule of k_brute_nearest.  Results are identical to
+// that kernel's.  Points or queries with non-finite coordinates or squared
+// norms above 1e30 are always candidates (exact path).
+constexpr int kTcTile = 512;       // points per shared-memory stage
+constexpr int64_t kTcMinPoints = 64; // fewer points: the plain kernel
+constexpr float kTcSlack = 1.52587890625e-05f; // e = 2^-16
+constexpr float kTcBig = 1e30f;
+
+__device__ __forceinline__ uint32_t tf32_rna(float x)
+{
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// D = A B + C for one m16n8k8 tile: lane (g, t) gives A[g][t], A[g + 8][t],
+// A[g][t + 4], A[g + 8][t + 4] and B[t][g], B[t + 4][g].
+__device__ __forceinline__ void mma_k8(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2,
+                                       uint32_t a3, uint32_t b0, uint32_t b1)
+{
+  asm volatile("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 "
+               "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+               : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+               : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+template <int K>
+__global__ void __launch_bounds__(kQueryThreads)
+    k_brute_nearest_tc(const float4 *__restrict__ values, int64_t n,
+                       const float *__restrict__ queries, int64_t nq,
+                       const int32_t *__restrict__ kq, int32_t k_all,
+                       const int32_t *__restrict__ offsets, int32_t *__restrict__ offsets_out,
+                       int32_t *__restrict__ out_idx, float *__restrict__ out_dist)
+{
+  constexpr unsigned kAll = 0xffffffffu;
+  constexpr int kWarps = kQueryThreads / 32;
+  __shared__ float4 s_pt[kTcTile];
+  __shared__ float4 s_hi[kTcTile];
+  __shared__ float4 s_lo[kTcTile];
+  __shared__ int s_cand[kWarps][32][8];
+  __shared__ int s_cnt[kWarps][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tq = lane & 3;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = t < nq;
+  KnnTask task{};
+  if (active)
+  {
+    QueryTree tree;
+    task = knn_task(t, n, ForestView{nullptr, nullptr, 1}, tree, nq, nullptr, kq, k_all,
+                    offsets, offsets_out);
+  }
+  const bool work = active && task.kk > 0;
+  uint64_t key[K];
+  const int first = K - (work ? task.k : 0);
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    key[j] = j < first ? 0ull : kKeyEmpty;
+  float thr = INFINITY;
+  float qx = 0, qy = 0, qz = 0;
+  if (work)
+  {
+    qx = __ldg(queries + 3 * task.q);
+    qy = __ldg(queries + 3 * task.q + 1);
+    qz = __ldg(queries + 3 * task.q + 2);
+  }
+  const float qn = __fadd_rn(__fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy)), __fmul_rn(qz, qz));
+  // a query outside the filter's range takes every pair (T = +inf, NaN pairs
+  // count as candidates through !(c > T))
+  const bool q_exact = !(qn <= kTcBig);
+  const float qn_lo = __fmul_rd(qn, 1.f - kTcSlack);
+  // the per-row bound the filter compares C' with
+  auto row_bound = [&]() -> float {
+    if (!work)
+      return -INFINITY;
+    if (q_exact || thr == INFINITY)
+      return INFINITY;
+    return __fsub_ru(thr, qn_lo);
+  };
+  float T = row_bound();
+  // A fragments of the rows g, g + 8, 16 + g, 24 + g: component tq of
+  // (qx, qy, qz, 1), high and low tf32 parts
+  uint32_t ahi[4], alo[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+  {
+    const int row = (r >> 1) * 16 + (r & 1) * 8 + g;
+    const float x = __shfl_sync(kAll, qx, row), y = __shfl_sync(kAll, qy, row),
+                z = __shfl_sync(kAll, qz, row);
+    const float a = tq == 0 ? x : tq == 1 ? y : tq == 2 ? z : 1.f;
+    ahi[r] = tf32_rna(a);
+    alo[r] = tf32_rna(__fsub_rn(a, __uint_as_float(ahi[r])));
+  }
+  float Trow[4];
+  auto load_bounds = [&]() {
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+      Trow[r] = __shfl_sync(kAll, T, (r >> 1) * 16 + (r & 1) * 8 + g);
+  };
+  load_bounds();
+  s_cnt[warp][lane] = 0;
+  auto offer = [&](float s, int v) {
+    if (s <= thr)
+    {
+      const uint64_t c = knn_key(__fsqrt_rn(s), v);
+      if (c < key[K - 1])
+      {
+        list_insert<K>(key, c);
+        if (key[K - 1] != kKeyEmpty)
+          thr = sq_bound(key_dist(key[K - 1]));
+      }
+    }
+  };
+  for (int64_t t0 = 0; t0 < n; t0 += kTcTile)
+  {
+    const int m = (int)min((int64_t)kTcTile, n - t0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < kTcTile; j += blockDim.x)
+    {
+      float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+      if (j < m)
+      {
+        p = __ldg(values + t0 + j);
+        const float pn =
+            __fadd_rn(__fadd_rn(__fmul_rn(p.x, p.x), __fmul_rn(p.y, p.y)), __fmul_rn(p.z, p.z));
+        if (pn <= kTcBig)
+        {
+          const float b[4] = {__fmul_rn(-2.f, p.x), __fmul_rn(-2.f, p.y), __fmul_rn(-2.f, p.z),
+                              __fmul_rn(pn, 1.f - kTcSlack)};
+          float h[4], l[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c)
+          {
+            h[c] = __uint_as_float(tf32_rna(b[c]));
+            l[c] = __uint_as_float(tf32_rna(__fsub_rn(b[c], h[c])));
+          }
+          hi = make_float4(h[0], h[1], h[2], h[3]);
+          lo = make_float4(l[0], l[1], l[2], l[3]);
+        }
+        else // outside the filter's range: C' = -FLT_MAX, always a candidate
+          hi.w = -FLT_MAX;
+      }
+      else
+        p.w = __int_as_float(-1); // padding: never offered
+      s_pt[j] = p;
+      s_hi[j] = hi;
+      s_lo[j] = lo;
+    }
+    __syncthreads();
+    for (int p0 = 0; p0 < m; p0 += 8)
+    {
+      const float *bh = reinterpret_cast<const float *>(s_hi + p0 + g);
+      const float *bl = reinterpret_cast<const float *>(s_lo + p0 + g);
+      const uint32_t bhi = __float_as_uint(bh[tq]), blo = __float_as_uint(bl[tq]);
+      float c[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+      for (int blk = 0; blk < 2; ++blk)
+      {
+        mma_k8(c[blk], ahi[2 * blk], ahi[2 * blk + 1], 0u, 0u, blo, 0u);
+        mma_k8(c[blk], ahi[2 * blk], ahi[2 * blk + 1], alo[2 * blk], alo[2 * blk + 1], bhi, bhi);
+      }
+      // c[blk][e]: row blk * 16 + (e >> 1) * 8 + g, point p0 + 2 tq + (e & 1)
+      unsigned mask = 0;
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        mask |= (unsigned)!(c[e >> 2][e & 3] > Trow[2 * (e >> 2) + ((e & 3) >> 1)]) << e;
+      if (__any_sync(kAll, mask != 0))
+      {
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+        {
+          const int row = (e >> 2) * 16 + ((e & 3) >> 1) * 8 + g;
+          const int pj = p0 + 2 * tq + (e & 1);
+          if (((mask >> e) & 1) && pj < m)
+          {
+            const int slot = atomicAdd(&s_cnt[warp][row], 1);
+            s_cand[warp][row][slot] = pj;
+          }
+        }
+        __syncwarp();
+        const int cnt = s_cnt[warp][lane];
+        for (int i = 0; i < cnt; ++i)
+        {
+          const float4 p = s_pt[s_cand[warp][lane][i]];
+          if (__float_as_int(p.w) >= 0)
+            offer(dist2_pp(qx, qy, qz, p.x, p.y, p.z), __float_as_int(p.w));
+        }
+        s_cnt[warp][lane] = 0;
+        T = row_bound();
+        __syncwarp();
+        load_bounds();
       }
     }
   }
@@ -722,7 +946,10 @@ abx_status nearest_k(cudaStream_t s, TreeView const &t, ForestView const &f,
   const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
   const int bucket =
       std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
-  if (!t.tnodes) // brute force
+  if (!t.tnodes && KIND == 0 && t.n >= kTcMinPoints && tuning_value("BRUTE_TENSOR", 1))
+    k_brute_nearest_tc<K><<<blocks, kQueryThreads, 0, s>>>(
+        t.sorted, t.n, d_queries, nq, d_k, k, d_offsets, d_offsets_out, d_idx, d_dist);
+  else if (!t.tnodes) // brute force
     k_brute_nearest<K, KIND><<<blocks, kQueryThreads, 0, s>>>(
         t.sorted, t.n, d_queries, nq, d_k, k, d_offsets, d_offsets_out, d_idx, d_dist);
   else if (bucket >= 2)

@@ -75,7 +75,7 @@ def parse():
     ap.add_argument("--kdop", type=int, default=14, choices=[6, 14, 18, 26],
                     help="--case kdop: KDOP<3, k> of the values")
     ap.add_argument("--case", default="knn",
-                    choices=["knn", "build", "nearest", "radius", "forest", "serve", "kdop"],
+                    choices=["knn", "build", "nearest", "radius", "forest", "serve", "kdop", "brute"],
                     help="knn: the benchmark step (build + kNN); build / nearest / radius: "
                     "one stage alone (profiling cases; radius = 2-pass CRS search with "
                     "~32 expected neighbours)")
@@ -544,12 +544,15 @@ def run_case(args):
     points = torch.from_numpy(points_np).cuda()
     queries = torch.from_numpy(queries_np).cuda()
     r = float(np.float32((32 * 3 / (4 * np.pi * args.n)) ** (1 / 3)))
-    bvh = ax.BoundingVolumeHierarchy(points) if args.case != "build" else None
+    if args.case == "brute":
+        bvh = ax.BruteForce(points)
+    else:
+        bvh = ax.BoundingVolumeHierarchy(points) if args.case != "build" else None
 
     def once():
         if args.case == "build":
             return ax.BoundingVolumeHierarchy(points)
-        if args.case == "nearest":
+        if args.case in ("nearest", "brute"):
             return ax.query(bvh, ax.nearest(queries, args.k))
         return ax.query(bvh, ax.make_intersects(queries, r))
 

@@ -75,3 +75,43 @@ def test_brute_empty_and_bounds(ax):
     p = uniform_points(100, 2)
     bf = ax.BruteForce(cuda(p))
     assert np.array_equal(bits(bf.bounds()), bits(np.concatenate([p.min(0), p.max(0)])))
+
+
+@pytest.mark.parametrize("case", ["uniform", "duplicates", "far", "nonfinite", "clustered"])
+@pytest.mark.parametrize("k", [1, 16, 32])
+def test_tensor_filter_equals_plain_brute_force(ax, case, k):
+    """The tensor-core candidate filter (BRUTE_TENSOR) returns exactly what
+    the plain brute-force kernel returns: ties, duplicates, coordinates far
+    from the origin (filter out of range), non-finite values, tight clusters."""
+    rng = np.random.default_rng({"uniform": 1, "duplicates": 2, "far": 3, "nonfinite": 4,
+                                 "clustered": 5}[case])
+    p = uniform_points(3000, 151)
+    q = uniform_points(700, 152)
+    if case == "duplicates":
+        p = np.repeat(p[:300], 10, axis=0)
+        q[::3] = p[::9][: len(q[::3])]
+    elif case == "far":
+        p = p * 1e16 + 3e16
+        q = q * 1e16 + 3e16
+    elif case == "nonfinite":
+        p[::97] = np.inf
+        q[::53, 1] = np.inf
+    elif case == "clustered":
+        p = (0.5 + 1e-3 * rng.standard_normal((3000, 3))).astype(np.float32)
+        q = (0.5 + 1e-3 * rng.standard_normal((700, 3))).astype(np.float32)
+    L = ax._lib.load()
+    bf = ax.BruteForce(cuda(p))
+    try:
+        ax._lib.check(L.abx_tuning_set(b"BRUTE_TENSOR", 1))
+        a = ax.query(bf, ax.nearest(cuda(q), k), with_distances=True)
+        ax._lib.check(L.abx_tuning_set(b"BRUTE_TENSOR", 0))
+        b = ax.query(bf, ax.nearest(cuda(q), k), with_distances=True)
+    finally:
+        L.abx_tuning_reset()
+    for x, y in zip(a, b):
+        assert torch.equal(x.view(torch.int32) if x.dtype == torch.float32 else x,
+                           y.view(torch.int32) if y.dtype == torch.float32 else y)
+    if case == "uniform":
+        bi, bd = o.knn_brute(p, q, k)
+        assert np.array_equal(a[0].cpu().numpy().reshape(len(q), k), bi)
+    assert ax.device_errors() == 0
