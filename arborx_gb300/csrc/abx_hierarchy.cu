@@ -966,7 +966,13 @@ abx_status forest_query_order(cudaStream_t s, abx_geometry pred_kind, const floa
     Scratch<uint32_t> keys;
     ABX_CUDA_TRY(keys.alloc(nq, s));
     ABX_QKEYS(uint32_t);
-    // big trees hold many queries per top-digit cell: the plain LSD sort
+    // the order only schedules the queries: the top three digits (tree, then
+    // the high Morton bits) suffice (4096 clouds, 5.85e7 box queries: order
+    // 2.91 vs 3.84 ms for all four digits, traversal 9.91 vs 9.82 ms); 0 asks
+    // for the full sort
+    const int digits = tuning_value("FOREST_ORDER_DIGITS", 3);
+    if (digits >= 1 && digits <= 3)
+      return radix_order_top_u32(s, keys.ptr, d_perm, nq, 4, nullptr, digits);
     return radix_sort_u32(s, keys.ptr, d_perm, nullptr, nq, 4, nullptr, 0);
   }
   Scratch<uint64_t> keys;
