@@ -1271,30 +1271,32 @@ abx_status abx_bvh_query_nearest_host(const abx_bvh *bvh, void *stream, const fl
     struct Copy
     {
       cudaStream_t st = nullptr;
-      cudaEvent_t in = nullptr, done = nullptr;
+      cudaEvent_t in = nullptr, off = nullptr, done = nullptr;
       ~Copy()
       {
-        if (in)
-          cudaEventDestroy(in);
-        if (done)
-          cudaEventDestroy(done);
+        for (cudaEvent_t e : {in, off, done})
+          if (e)
+            cudaEventDestroy(e);
         if (st)
           cudaStreamDestroy(st);
       }
     } c;
     ABX_CUDA_TRY(cudaStreamCreateWithFlags(&c.st, cudaStreamNonBlocking));
     ABX_CUDA_TRY(cudaEventCreateWithFlags(&c.in, cudaEventDisableTiming));
+    ABX_CUDA_TRY(cudaEventCreateWithFlags(&c.off, cudaEventDisableTiming));
     ABX_CUDA_TRY(cudaEventCreateWithFlags(&c.done, cudaEventDisableTiming));
     Scratch<float> dq; // allocated and released on the copy stream
     ABX_CUDA_TRY(dq.alloc((size_t)nq * 3, c.st));
     ABX_CUDA_TRY(cudaMemcpyAsync(dq.ptr, h_queries, (size_t)nq * 3 * sizeof(float),
                                  cudaMemcpyHostToDevice, c.st));
     ABX_CUDA_TRY(cudaEventRecord(c.in, c.st));
+    // the offsets (a fixed k) go to the host alongside the traversal
+    ABX_TRY(fill_offsets_iota(c.st, static_cast<int32_t *>(dev_off), nq + 1, 0, kk));
+    ABX_CUDA_TRY(cudaEventRecord(c.off, c.st));
     ABX_CUDA_TRY(cudaStreamWaitEvent(s, c.in, 0));
     abx_status st = nearest_into(bvh, s, dq.ptr, nq, k, policy, false, nullptr,
                                  static_cast<int32_t *>(dev_idx), static_cast<float *>(dev_dist));
-    if (st == ABX_SUCCESS)
-      st = fill_offsets_iota(s, static_cast<int32_t *>(dev_off), nq + 1, 0, kk);
+    cudaStreamWaitEvent(s, c.off, 0);
     // the copy stream frees the queries after the traversal read them
     cudaEventRecord(c.done, s);
     cudaStreamWaitEvent(c.st, c.done, 0);
