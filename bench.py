@@ -67,6 +67,7 @@ def parse():
     ap.add_argument("--no-plain", action="store_true",
                     help="--case forest: time the batched arm only")
     ap.add_argument("--serve-requests", type=int, default=2000)
+    ap.add_argument("--workers", type=int, default=4, help="--case serve: concurrent batches")
     ap.add_argument("--l2-persist", action="store_true",
                     help="--case serve: L2-persisting window on the queried tree's nodes")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[500, 2000, 8000, 32000])
@@ -786,7 +787,7 @@ def run_serve(args):
                          device="cuda")
         trees.append(ax.BoundingVolumeHierarchy(pts))
     torch.cuda.synchronize()
-    srv = ax.Server(workers=4, l2_persist=args.l2_persist)
+    srv = ax.Server(workers=args.workers, l2_persist=args.l2_persist)
     tids = [srv.add_tree(t) for t in trees]
     radius = (32 * 3 / (4 * np.pi * sizes.astype(np.float64))) ** (1 / 3)
     rng = np.random.default_rng(17)
@@ -834,7 +835,7 @@ def run_serve(args):
         })
     srv.close()
     print(json.dumps({
-        "case": "serve", "trees": ntrees, "points": int(sizes.sum()), "workers": 4,
+        "case": "serve", "trees": ntrees, "points": int(sizes.sum()), "workers": args.workers,
         "l2_persist": bool(args.l2_persist),
         "requests_per_rate": len(pool), "sweep": sweep,
     }), flush=True)
