@@ -883,6 +883,50 @@ size_t tree_kleaf_count(int ndir, int64_t n)
 {
   return ndir ? (size_t)std::max<int64_t>(n, 1) * (kdop_pad(ndir) / 4) : 0;
 }
+
+// Every reference a traversal follows stays inside the tree: a file read
+// from disk is checked before it reaches the device (the kernels' own
+// range checks stop walks, but a bucket scan reads leaf positions
+// [start, start + count) straight from a node's count field).
+bool valid_tree_arrays(const std::vector<TNode> &tn, const std::vector<float4> &so, int64_t n,
+                       int leaf_float4s)
+{
+  const int64_t nt = (int64_t)tn.size();
+  for (int64_t t = 0; t < n; ++t)
+  {
+    int v;
+    std::memcpy(&v, &so[(size_t)(t * leaf_float4s)].w, sizeof(int));
+    if (v < 0 || v >= n)
+      return false;
+  }
+  for (int64_t i = 0; i < nt; ++i)
+  {
+    const int refs[2] = {tn[i].d.x, tn[i].d.y}, cfs[2] = {tn[i].d.z, tn[i].d.w};
+    for (int side = 0; side < 2; ++side)
+    {
+      const int ref = refs[side], cf = cfs[side];
+      if (ref < 0)
+      {
+        const int64_t v = bucket_start(ref);
+        const bool absent = n == 1 && side == 1 && cf == 0; // one-leaf tree
+        if (!absent && (cf != 1 || v >= n))
+          return false;
+        continue;
+      }
+      if (ref >= nt || (cf & ~(0xffff | kBucketRightEnd)) != 0)
+        return false;
+      const int c = cf & 0xffff;
+      if (c == 0)
+        continue;
+      if (c < 2 || c > kMaxBucket)
+        return false;
+      const int64_t start = (cf & kBucketRightEnd) ? (int64_t)ref - c + 1 : ref;
+      if (start < 0 || start + c > n)
+        return false;
+    }
+  }
+  return true;
+}
 } // namespace
 
 abx_status abx_bvh_save(const abx_bvh *bvh, const char *path)
@@ -945,6 +989,8 @@ abx_status abx_bvh_load(void *stream, const char *path, abx_bvh **out)
        (nkn == 0 || std::fread(kn.data(), sizeof(float4), nkn, f) == nkn) &&
        (nkl == 0 || std::fread(kl.data(), sizeof(float4), nkl, f) == nkl);
   std::fclose(f);
+  if (ok)
+    ok = valid_tree_arrays(tn, so, h.n, kind == ABX_BOX ? 2 : 1);
   if (!ok)
     return fail(ABX_ERROR_INVALID_ARGUMENT, std::string("abx_bvh_load: not a tree file: ") + path);
   device_state();

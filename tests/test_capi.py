@@ -87,3 +87,48 @@ def test_tree_file_errors_are_reported_on_the_host(tmp_path):
     assert L.abx_bvh_load(None, str(bad).encode(), ctypes.byref(h)) == 1
     assert not h.value
     assert L.abx_bvh_save(None, missing) == 1
+
+
+def test_tree_file_with_bad_references_is_refused(tmp_path):
+    """A tree file whose node references leave the tree (a corrupted or
+    hostile file) is refused on the host before anything reaches the device."""
+    import ctypes
+    import struct
+
+    import numpy as np
+
+    from arborx_gb300 import _lib
+
+    L = _lib.load()
+    n = 3
+
+    def write(nodes, leaves):
+        hdr = b"ABXBVH01" + struct.pack("<iiq6f", 0, 0, n, 0, 0, 0, 1, 1, 1)
+        body = nodes.tobytes() + leaves.tobytes()
+        path = tmp_path / "t.abx"
+        path.write_bytes(hdr + body)
+        return str(path).encode()
+
+    def node(lref, rref, lc, rc):
+        a = np.zeros(16, np.int32)
+        a[12:16] = [lref, rref, lc, rc]
+        return a
+
+    leaves = np.zeros((n, 4), np.float32)
+    leaves[:, 3] = np.arange(n, dtype=np.int32).view(np.float32)
+    h = ctypes.c_void_p()
+    bad_sets = [
+        # internal reference past the node array
+        np.concatenate([node(5, ~2, 2, 1), node(~0, ~1, 1, 1)]),
+        # leaf value past the leaves
+        np.concatenate([node(1, ~7, 2, 1), node(~0, ~1, 1, 1)]),
+        # bucket count running past the leaves
+        np.concatenate([node(1, ~2, 30, 1), node(~0, ~1, 1, 1)]),
+    ]
+    for nodes in bad_sets:
+        assert L.abx_bvh_load(None, write(nodes, leaves), ctypes.byref(h)) == 1
+        assert not h.value
+    bad_leaves = leaves.copy()
+    bad_leaves[1, 3] = np.array([9], np.int32).view(np.float32)[0]
+    good_nodes = np.concatenate([node(1, ~2, 2, 1), node(~0, ~1, 1, 1)])
+    assert L.abx_bvh_load(None, write(good_nodes, bad_leaves), ctypes.byref(h)) == 1
