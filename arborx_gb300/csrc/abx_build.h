@@ -91,6 +91,10 @@ struct TreeView
   int ndir = 0;
   const float *knodes = nullptr;
   const float *kleaves = nullptr;
+  // brute force over points: the values again in Morton order ({x, y, z,
+  // value}) with their sorted Morton64 codes (scan start of a query block)
+  const float4 *morton_sorted = nullptr;
+  const uint64_t *morton_codes = nullptr;
 };
 
 // Trees of a batch seen by a query launch: tree s owns the sorted positions
@@ -207,6 +211,11 @@ abx_status launch_nearest(cudaStream_t s, TreeView const &t, ForestView const *f
 // outside [0, n_src) raise the device error word and give zeros).
 abx_status gather_rows(cudaStream_t s, const void *d_src, int64_t n_src, int words,
                        const int32_t *d_rows, int64_t m, void *d_dst);
+
+// d_out[i] = {point d_g[d_perm[i]], value d_perm[i]} (brute force in Morton
+// order).
+abx_status brute_pack_sorted(cudaStream_t s, const float *d_g, const uint32_t *d_perm, int64_t n,
+                             float4 *d_out);
 
 // d_out[i] = (first + i) * step for i < count (CRS offsets of a fixed k).
 abx_status fill_offsets_iota(cudaStream_t s, int32_t *d_out, int64_t count, int64_t first,

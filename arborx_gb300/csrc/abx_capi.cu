@@ -44,6 +44,9 @@ struct abx_bvh
   abx_geometry kdop_kind = ABX_BOX;
   float4 *knodes = nullptr;
   float4 *kleaves = nullptr;
+  // brute force over points: values in Morton order and their codes
+  float4 *morton_sorted = nullptr;
+  uint64_t *morton_codes = nullptr;
 };
 
 struct abx_forest : abx_bvh
@@ -257,6 +260,8 @@ void destroy_tree(abx_bvh *t)
   dfree(t->d_off, s);
   dfree(t->knodes, s);
   dfree(t->kleaves, s);
+  dfree(t->morton_sorted, s);
+  dfree(t->morton_codes, s);
   if (t->h_bounds)
   {
     if (t->ready)
@@ -386,6 +391,8 @@ TreeView view_of(const abx_bvh *t)
   v.ndir = t->ndir;
   v.knodes = reinterpret_cast<const float *>(t->knodes);
   v.kleaves = reinterpret_cast<const float *>(t->kleaves);
+  v.morton_sorted = t->morton_sorted;
+  v.morton_codes = t->morton_codes;
   return v;
 }
 
@@ -579,7 +586,7 @@ abx_status query_nearest(const abx_bvh *bvh, cudaStream_t s, const float *d_quer
   }
   const ForestView *f = h_qoff ? &fv : nullptr;
   Scratch<uint32_t> perm;
-  if (policy.sort_predicates && nq > 1 && bvh->tnodes)
+  if (policy.sort_predicates && nq > 1 && (bvh->tnodes || bvh->morton_sorted))
   {
     abx_status st = sort_predicates(s, bvh, ABX_POINT, d_queries, nq, qoff.ptr, perm);
     if (st != ABX_SUCCESS)
@@ -1673,6 +1680,9 @@ abx_status abx_forest_query_nearest(const abx_forest *forest, void *stream,
                        with_distances, out);
 }
 
+// Brute-force point sets from this size on keep a Morton-ordered copy.
+constexpr int64_t kBruteMortonMin = 64;
+
 abx_status abx_brute_create(void *stream, abx_geometry kind, const float *d_values, int64_t n,
                             abx_brute **out)
 {
@@ -1711,6 +1721,25 @@ abx_status abx_brute_create(void *stream, abx_geometry kind, const float *d_valu
     st = scene_bounds(s, kind, d_values, n, t->d_bounds);
     if (st == ABX_SUCCESS)
       st = brute_pack(s, kind, d_values, n, t->sorted);
+    if (st == ABX_SUCCESS && kind == ABX_POINT && n >= kBruteMortonMin)
+    {
+      // the points again in Morton order for the tensor-core filter's
+      // coherent scan (nearest); intersects keep the input order
+      Scratch<uint32_t> perm, hist;
+      if (dmalloc_n(&t->morton_codes, (size_t)n, s) != cudaSuccess ||
+          dmalloc_n(&t->morton_sorted, (size_t)n, s) != cudaSuccess ||
+          perm.alloc((size_t)n, s) != cudaSuccess || hist.alloc(8 * 256, s) != cudaSuccess)
+        st = fail(ABX_ERROR_OUT_OF_MEMORY, "abx_brute_create: device allocation");
+      if (st == ABX_SUCCESS && cudaMemsetAsync(hist.ptr, 0, 8 * 256 * sizeof(uint32_t), s) != cudaSuccess)
+        st = fail(ABX_ERROR_CUDA, "abx_brute_create: memset");
+      if (st == ABX_SUCCESS)
+        st = morton64_codes(s, kind, d_values, n, t->d_bounds, t->morton_codes, hist.ptr);
+      if (st == ABX_SUCCESS)
+        st = radix_sort_u64(s, t->morton_codes, perm.ptr, nullptr, n, 8, hist.ptr,
+                            stream_capturing(s) ? 0 : hybrid_top_passes(n, 8));
+      if (st == ABX_SUCCESS)
+        st = brute_pack_sorted(s, d_values, perm.ptr, n, t->morton_sorted);
+    }
     if (st == ABX_SUCCESS &&
         cudaMemcpyAsync(t->h_bounds, t->d_bounds, 6 * sizeof(float), cudaMemcpyDeviceToHost, s) !=
             cudaSuccess)

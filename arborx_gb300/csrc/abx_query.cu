@@ -598,7 +598,11 @@ __global__ void __launch_bounds__(kQueryThreads)
 }
 
 // Nearest over point values with the all-pairs product on tensor cores as a
-// candidate filter (mma.sync m16n8k8 tf32).  A warp owns 32 queries; per
+// candidate filter (mma.sync m16n8k8 tf32).  The points are scanned in
+// Morton order, each CTA starting at the tile where the Morton64 code of its
+// first query falls and wrapping around: with the queries in Morton order too,
+// a query's list reaches its final neighbours within the first tiles, so
+// later tiles rarely produce candidates.  A warp owns 32 queries; per
 // group of 8 points it forms, for its two 16-query row blocks,
 //   C'(q, p) = |p|^2 (1 - e) - 2 q.p,   e = 2^-16,
 // from A rows (qx, qy, qz, 1) and B columns (-2px, -2py, -2pz, |p|^2 (1 - e))
@@ -613,8 +617,7 @@ __global__ void __launch_bounds__(kQueryThreads)
 // exact formula and key rule of k_brute_nearest.  Results are identical to
 // that kernel's.  Points or queries with non-finite coordinates or squared
 // norms above 1e30 are always candidates (exact path).
-constexpr int kTcTile = 512;       // points per shared-memory stage
-constexpr int64_t kTcMinPoints = 64; // fewer points: the plain kernel
+constexpr int kTcTile = 512; // points per shared-memory stage
 constexpr float kTcSlack = 1.52587890625e-05f; // e = 2^-16
 constexpr float kTcBig = 1e30f;
 
@@ -639,7 +642,9 @@ __device__ __forceinline__ void mma_k8(float (&c)[4], uint32_t a0, uint32_t a1, 
 template <int K>
 __global__ void __launch_bounds__(kQueryThreads)
     k_brute_nearest_tc(const float4 *__restrict__ values, int64_t n,
+                       const uint64_t *__restrict__ codes, const float *__restrict__ scene,
                        const float *__restrict__ queries, int64_t nq,
+                       const uint32_t *__restrict__ perm,
                        const int32_t *__restrict__ kq, int32_t k_all,
                        const int32_t *__restrict__ offsets, int32_t *__restrict__ offsets_out,
                        int32_t *__restrict__ out_idx, float *__restrict__ out_dist)
@@ -651,6 +656,7 @@ __global__ void __launch_bounds__(kQueryThreads)
   __shared__ float4 s_lo[kTcTile];
   __shared__ int s_cand[kWarps][32][8];
   __shared__ int s_cnt[kWarps][32];
+  __shared__ int64_t s_start;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane >> 2, tq = lane & 3;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -659,7 +665,7 @@ __global__ void __launch_bounds__(kQueryThreads)
   if (active)
   {
     QueryTree tree;
-    task = knn_task(t, n, ForestView{nullptr, nullptr, 1}, tree, nq, nullptr, kq, k_all,
+    task = knn_task(t, n, ForestView{nullptr, nullptr, 1}, tree, nq, perm, kq, k_all,
                     offsets, offsets_out);
   }
   const bool work = active && task.kk > 0;
@@ -676,6 +682,31 @@ __global__ void __launch_bounds__(kQueryThreads)
     qy = __ldg(queries + 3 * task.q + 1);
     qz = __ldg(queries + 3 * task.q + 2);
   }
+  // the tile of the first query's Morton code: the CTA's scan starts there
+  if (threadIdx.x == 0)
+  {
+    int64_t pos = 0;
+    if (active)
+    {
+      const uint64_t c = morton64_unit(translate_scale(qx, __ldg(scene), __ldg(scene + 3)),
+                                       translate_scale(qy, __ldg(scene + 1), __ldg(scene + 4)),
+                                       translate_scale(qz, __ldg(scene + 2), __ldg(scene + 5)));
+      int64_t a = 0, b = n; // first position with code >= c
+      while (a < b)
+      {
+        const int64_t mid = (a + b) >> 1;
+        if (__ldg(codes + mid) < c)
+          a = mid + 1;
+        else
+          b = mid;
+      }
+      pos = a;
+    }
+    s_start = pos;
+  }
+  __syncthreads();
+  const int64_t num_tiles = (n + kTcTile - 1) / kTcTile;
+  const int64_t start_tile = min(s_start / kTcTile, num_tiles - 1);
   const float qn = __fadd_rn(__fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy)), __fmul_rn(qz, qz));
   // a query outside the filter's range takes every pair (T = +inf, NaN pairs
   // count as candidates through !(c > T))
@@ -723,8 +754,12 @@ __global__ void __launch_bounds__(kQueryThreads)
       }
     }
   };
-  for (int64_t t0 = 0; t0 < n; t0 += kTcTile)
+  for (int64_t it = 0; it < num_tiles; ++it)
   {
+    int64_t tile = start_tile + it;
+    if (tile >= num_tiles)
+      tile -= num_tiles;
+    const int64_t t0 = tile * kTcTile;
     const int m = (int)min((int64_t)kTcTile, n - t0);
     __syncthreads();
     for (int j = threadIdx.x; j < kTcTile; j += blockDim.x)
@@ -887,6 +922,19 @@ __global__ void __launch_bounds__(kQueryThreads)
   }
 }
 
+// Points in Morton order for the filtered brute force: {x, y, z, index}.
+__global__ void k_brute_pack_sorted(const float *__restrict__ g, const uint32_t *__restrict__ perm,
+                                    int64_t n, float4 *__restrict__ out)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+  {
+    const uint32_t v = __ldg(perm + i);
+    out[i] = make_float4(__ldg(g + 3 * (int64_t)v), __ldg(g + 3 * (int64_t)v + 1),
+                         __ldg(g + 3 * (int64_t)v + 2), __int_as_float((int)v));
+  }
+}
+
 // Pack values in input order: {x, y, z, index} (two float4 per box).
 template <int KIND>
 __global__ void k_brute_pack(const float *__restrict__ g, int64_t n, float4 *__restrict__ values)
@@ -946,9 +994,10 @@ abx_status nearest_k(cudaStream_t s, TreeView const &t, ForestView const &f,
   const unsigned blocks = (unsigned)((nq + kQueryThreads - 1) / kQueryThreads);
   const int bucket =
       std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
-  if (!t.tnodes && KIND == 0 && t.n >= kTcMinPoints && tuning_value("BRUTE_TENSOR", 1))
+  if (!t.tnodes && t.morton_sorted && tuning_value("BRUTE_TENSOR", 1))
     k_brute_nearest_tc<K><<<blocks, kQueryThreads, 0, s>>>(
-        t.sorted, t.n, d_queries, nq, d_k, k, d_offsets, d_offsets_out, d_idx, d_dist);
+        t.morton_sorted, t.n, t.morton_codes, t.d_bounds, d_queries, nq, d_perm, d_k, k, d_offsets,
+        d_offsets_out, d_idx, d_dist);
   else if (!t.tnodes) // brute force
     k_brute_nearest<K, KIND><<<blocks, kQueryThreads, 0, s>>>(
         t.sorted, t.n, d_queries, nq, d_k, k, d_offsets, d_offsets_out, d_idx, d_dist);
@@ -1035,6 +1084,16 @@ abx_status launch_spatial(cudaStream_t s, TreeView const &t, ForestView const *f
                       : spatial_dispatch<ABX_RAY, 0>(s, t, f, d_preds, nq, d_perm, mode, d_counts,
                                                      d_offsets, d_out, buffer, d_overflow);
   return fail(ABX_ERROR_INVALID_ARGUMENT, "intersects predicates must be spheres, boxes, rays or KDOPs");
+}
+
+abx_status brute_pack_sorted(cudaStream_t s, const float *d_g, const uint32_t *d_perm, int64_t n,
+                             float4 *d_out)
+{
+  if (n <= 0)
+    return ABX_SUCCESS;
+  k_brute_pack_sorted<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_g, d_perm, n, d_out);
+  ABX_CUDA_TRY(cudaGetLastError());
+  return ABX_SUCCESS;
 }
 
 abx_status brute_pack(cudaStream_t s, abx_geometry kind, const float *d_g, int64_t n,
