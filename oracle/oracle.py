@@ -417,3 +417,33 @@ def in_tree_order(offsets, indices, leaf_values):
         row = indices[a:b]
         out[a:b] = row[np.argsort(pos[row], kind="stable")]
     return out
+
+
+def expand_half_to_full(offsets, indices):
+    """ArborX::Details::expandHalfToFull (src/spatial/detail/
+    ArborX_ExpandHalfToFull.hpp:23-69): every pair (i, k) of the half list
+    counts in rows i and k, an exclusive scan gives the offsets, and the pair
+    writes k into row i and i into row k.  Pure Python (small cases); rows in
+    insertion order (the reference fills them through atomics, so only their
+    contents are defined)."""
+    offsets = [int(x) for x in offsets]
+    indices = [int(x) for x in indices]
+    n = len(offsets) - 1
+    counts = [0] * (n + 1)
+    for i in range(n):
+        for j in range(offsets[i], offsets[i + 1]):
+            counts[i] += 1
+            counts[indices[j]] += 1
+    out_off = [0]
+    for i in range(n):
+        out_off.append(out_off[-1] + counts[i])
+    pos = out_off[:-1]
+    out = [0] * out_off[-1]
+    for i in range(n):
+        for j in range(offsets[i], offsets[i + 1]):
+            k = indices[j]
+            out[pos[i]] = k
+            pos[i] += 1
+            out[pos[k]] = i
+            pos[k] += 1
+    return out_off, out

@@ -266,6 +266,95 @@ def kdops(root):
                      "empty": {"indices": ints(sol[0][0]), "offsets": ints(sol[0][1])},
                      "query": {"indices": ints(sol[1][0]), "offsets": ints(sol[1][1])}}}
 
+
+def _geometry_literal(txt, env):
+    """A geometry argument of a reference test: Box{}, Box{{{..}}, {{..}}},
+    Point{..} / Point{{..}}, or a named constant of the test case."""
+    import math
+
+    t = txt.strip()
+    if t in env:
+        return env[t]
+    nums = [float(x) for x in re.findall(r"-?[0-9]*\.?[0-9]+(?:e-?[0-9]+)?", t)]
+    if t.startswith("Box{}"):
+        return ("box", "empty")
+    if t.startswith("Box"):
+        assert len(nums) == 6, t
+        return ("box", nums)
+    if t.startswith("Point"):
+        assert len(nums) == 3, t
+        return ("point", nums)
+    raise ValueError(t + " " + str(math.pi))
+
+
+def _split_args(call):
+    depth, cur, out = 0, "", []
+    for ch in call:
+        if ch in "({":
+            depth += 1
+        elif ch in ")}":
+            depth -= 1
+        if ch == "," and depth == 0:
+            out.append(cur)
+            cur = ""
+        else:
+            cur += ch
+    out.append(cur)
+    return out
+
+
+def geometry(root):
+    """test/tstGeometryIntersects.cpp:44-126 (point-box, box-box, sphere-point,
+    sphere-box; both argument orders must agree, as sym_intersects checks)
+    and test/tstGeometryDistance.cpp:39-67 (point-point and point-box
+    distances, compared exactly with float std::sqrt)."""
+    src = _read(root, "test/tstGeometryIntersects.cpp")
+    cases = []
+    for name, env in (("intersects_point_box", {"point": ("point", [1.0, 1.0, 1.0])}),
+                      ("intersects_box_box", {"box": ("box", [0, 0, 0, 1, 1, 1])}),
+                      ("intersects_sphere_point", {"sphere": ("sphere", [0, 0, 0, 1.0])}),
+                      ("intersects_sphere_box", {"sphere": ("sphere", [0, 0, 0, 1.0])})):
+        body = src[src.index("BOOST_AUTO_TEST_CASE_TEMPLATE(" + name + ","):]
+        body = body[:body.index("\n}\n")]
+        flat = re.sub(r"\s+", " ", body)
+        for m in re.finditer(r"(?:static_assert|BOOST_TEST)\( ?(!?)sym_intersects\(", flat):
+            i = m.end()
+            depth, j = 1, i
+            while depth:
+                depth += {"(": 1, ")": -1}.get(flat[j], 0)
+                j += 1
+            a, b = _split_args(flat[i:j - 1])
+            cases.append({"a": _geometry_literal(a, env), "b": _geometry_literal(b, env),
+                          "expected": m.group(1) == ""})
+    assert len(cases) == 4 + 13 + 5 + 2, len(cases)
+    dsrc = _read(root, "test/tstGeometryDistance.cpp")
+    dist = []
+    body = dsrc[dsrc.index("BOOST_AUTO_TEST_CASE_TEMPLATE(distance_point_point,"):
+                dsrc.index("BOOST_AUTO_TEST_CASE_TEMPLATE(distance_point_sphere,")]
+    flat = re.sub(r"\s+", " ", body)
+    env = {"box": ("box", [0, 0, 0, 1, 1, 1])}
+    for m in re.finditer(r"BOOST_TEST\(sym_distance\((.*?)\) == (std::sqrt\(\(Coordinate\)([0-9]+)\)|[0-9]+)\);", flat):
+        a, b = _split_args(m.group(1))
+        want = {"sqrt_of": int(m.group(3))} if m.group(3) else {"value": float(m.group(2))}
+        dist.append({"a": _geometry_literal(a, env), "b": _geometry_literal(b, env), "expected": want})
+    assert len(dist) == 6, len(dist)
+    return {"cite": "test/tstGeometryIntersects.cpp:44-126, test/tstGeometryDistance.cpp:39-67",
+            "intersects": cases, "distance": dist}
+
+
+def expand_half_to_full(root):
+    """test/tstDetailsExpandHalfToFull.cpp:48-80."""
+    src = _read(root, "test/tstDetailsExpandHalfToFull.cpp")
+    body = src[src.index("BOOST_AUTO_TEST_CASE_TEMPLATE(expand_half_to_full,"):]
+    flat = re.sub(r"\s+", " ", body)
+    vec = r"\(std::vector<int>\{([0-9, ]*)\}\)"
+    ints = lambda t: [int(v) for v in t.replace(" ", "").split(",") if v]
+    cases = [{"offsets_in": ints(a), "indices_in": ints(b), "offsets_out": ints(c), "indices_out": ints(d)}
+             for a, b, c, d in re.findall(r"ARBORX_TEST_EXPAND_HALF_TO_FULL\( ?exec_space, " + vec + ", " + vec
+                                          + ", " + vec + ", " + vec + r"\)", flat)]
+    assert len(cases) == 5, len(cases)
+    return {"cite": "test/tstDetailsExpandHalfToFull.cpp:48-80", "cases": cases}
+
 def main(root):
     data = {
         "source": "ArborX 2.1.99 test sources (read as text)",
@@ -277,6 +366,8 @@ def main(root):
         "neighbor_lists": neighbor_lists(root),
         "rays": rays(root),
         "kdops": kdops(root),
+        "geometry": geometry(root),
+        "expand_half_to_full": expand_half_to_full(root),
         "stack_capacity": {"cite": "tstQueryTreeDegenerate.cpp:367-446", "n": 4096},
         "manufactured_grid": {"cite": "tstQueryTreeManufacturedSolution.cpp:64-269", "nx": 11, "L": 100.0},
     }

@@ -305,3 +305,49 @@ def test_oracle_kdop_conversions():
     # an inverted box leaves the KDOP empty (ArborX_Expand.hpp:163-165)
     bad = np.array([[1, 0, 0, 0, 1, 1]], np.float32)
     assert np.array_equal(o.kdop_from_geometry(bad, 7, is_box=True)[0], o.kdop_empty(7))
+
+
+def _golden_geometry(g):
+    kind, v = g
+    if kind == "box" and v == "empty":
+        return "box", np.array([[np.float32(3.40282347e38)] * 3 + [np.float32(-3.40282347e38)] * 3],
+                               np.float32)
+    return kind, np.asarray([v], np.float32)
+
+
+def test_oracle_geometry_golden(golden):
+    """test/tstGeometryIntersects.cpp:44-126 and test/tstGeometryDistance.cpp:
+    39-67 through the oracle's brute force (one value, one predicate; a point
+    predicate is the degenerate box [p, p])."""
+    g = golden["geometry"]
+    for c in g["intersects"]:
+        got = []
+        for a, b in ((c["a"], c["b"]), (c["b"], c["a"])):
+            vk, vals = _golden_geometry(a)
+            pk, pred = _golden_geometry(b)
+            if vk == "sphere":
+                continue  # values are points or boxes
+            if pk == "point":
+                pk, pred = "box", np.concatenate([pred, pred], axis=1)
+            kind = o.KIND_SPHERE if pk == "sphere" else o.KIND_BOX
+            off, _ = o.spatial_brute(vals, kind, pred, is_box=vk == "box")
+            got.append(bool(off[-1]))
+        assert got and all(x == c["expected"] for x in got), c
+    for c in g["distance"]:
+        _, q = _golden_geometry(c["a"])
+        bk, vals = _golden_geometry(c["b"])
+        _, d = o.knn_brute(vals, q, 1, is_box=bk == "box")
+        e = c["expected"]
+        want = np.sqrt(np.float32(e["sqrt_of"])) if "sqrt_of" in e else np.float32(e["value"])
+        assert d[0, 0] == want, c
+
+
+def test_oracle_expand_half_to_full_golden(golden):
+    """test/tstDetailsExpandHalfToFull.cpp:48-80 (rows compared as multisets,
+    as the reference does)."""
+    for c in golden["expand_half_to_full"]["cases"]:
+        off, ind = o.expand_half_to_full(c["offsets_in"], c["indices_in"])
+        assert off == c["offsets_out"]
+        rows = [sorted(ind[off[i]:off[i + 1]]) for i in range(len(off) - 1)]
+        want = [sorted(c["indices_out"][off[i]:off[i + 1]]) for i in range(len(off) - 1)]
+        assert rows == want
