@@ -856,6 +856,157 @@ __global__ void __launch_bounds__(kQueryThreads)
   }
 }
 
+// intersects(Sphere) over point values with the same tensor-core filter:
+// the pair (q, p) can match only if |q|^2 (1 - e) + C'(q, p) <= r2, r2 the
+// query's exact squared-radius threshold; passing pairs are marked per query
+// in a shared-memory bit mask (one bit per point of the 8-point group) and
+// the owner lane tests them exactly in ascending point order, so the matches
+// come out in ascending value order like k_brute_spatial's (the points are
+// scanned in input order).
+template <int MODE>
+__global__ void __launch_bounds__(kQueryThreads)
+    k_brute_spatial_tc(const float4 *__restrict__ values, int64_t n,
+                       const float *__restrict__ preds, int64_t nq,
+                       const uint32_t *__restrict__ list, int32_t *__restrict__ counts,
+                       const int32_t *__restrict__ offsets, int32_t *__restrict__ out,
+                       int32_t buffer, unsigned *__restrict__ overflow)
+{
+  constexpr unsigned kAll = 0xffffffffu;
+  constexpr int kWarps = kQueryThreads / 32;
+  __shared__ float4 s_pt[kTcTile];
+  __shared__ float4 s_hi[kTcTile];
+  __shared__ float4 s_lo[kTcTile];
+  __shared__ unsigned s_mask[kWarps][32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tq = lane & 3;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = t < nq;
+  const int64_t q = active && list ? (int64_t)__ldg(list + t) : t;
+  float qx = 0.f, qy = 0.f, qz = 0.f, r2 = -1.f;
+  if (active)
+  {
+    const SpherePred sp = PredOf<ABX_SPHERE>::load(preds, q);
+    qx = sp.cx;
+    qy = sp.cy;
+    qz = sp.cz;
+    r2 = sp.r2;
+  }
+  int32_t *dst = nullptr;
+  if (MODE == kFill && active)
+    dst = out + __ldg(offsets + q);
+  if (MODE == kBuffered && active)
+    dst = out + q * (int64_t)buffer;
+  int32_t count = 0;
+  const float qn = __fadd_rn(__fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy)), __fmul_rn(qz, qz));
+  // r2 < 0 (negative radius) matches nothing; a query outside the filter's
+  // range takes every pair (NaN pairs count through !(c > T))
+  float T = -INFINITY;
+  if (active && r2 >= 0.f)
+    T = qn <= kTcBig ? __fsub_ru(r2, __fmul_rd(qn, 1.f - kTcSlack)) : INFINITY;
+  uint32_t ahi[4], alo[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+  {
+    const int row = (r >> 1) * 16 + (r & 1) * 8 + g;
+    const float x = __shfl_sync(kAll, qx, row), y = __shfl_sync(kAll, qy, row),
+                z = __shfl_sync(kAll, qz, row);
+    const float a = tq == 0 ? x : tq == 1 ? y : tq == 2 ? z : 1.f;
+    ahi[r] = tf32_rna(a);
+    alo[r] = tf32_rna(__fsub_rn(a, __uint_as_float(ahi[r])));
+  }
+  float Trow[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    Trow[r] = __shfl_sync(kAll, T, (r >> 1) * 16 + (r & 1) * 8 + g);
+  s_mask[warp][lane] = 0;
+  for (int64_t t0 = 0; t0 < n; t0 += kTcTile)
+  {
+    const int m = (int)min((int64_t)kTcTile, n - t0);
+    __syncthreads();
+    for (int j = threadIdx.x; j < kTcTile; j += blockDim.x)
+    {
+      float4 p = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+      float4 hi = make_float4(0.f, 0.f, 0.f, 0.f), lo = hi;
+      if (j < m)
+      {
+        p = __ldg(values + t0 + j);
+        const float pn =
+            __fadd_rn(__fadd_rn(__fmul_rn(p.x, p.x), __fmul_rn(p.y, p.y)), __fmul_rn(p.z, p.z));
+        if (pn <= kTcBig)
+        {
+          const float b[4] = {__fmul_rn(-2.f, p.x), __fmul_rn(-2.f, p.y), __fmul_rn(-2.f, p.z),
+                              __fmul_rn(pn, 1.f - kTcSlack)};
+          float h[4], l[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c)
+          {
+            h[c] = __uint_as_float(tf32_rna(b[c]));
+            l[c] = __uint_as_float(tf32_rna(__fsub_rn(b[c], h[c])));
+          }
+          hi = make_float4(h[0], h[1], h[2], h[3]);
+          lo = make_float4(l[0], l[1], l[2], l[3]);
+        }
+        else
+          hi.w = -FLT_MAX;
+      }
+      s_pt[j] = p;
+      s_hi[j] = hi;
+      s_lo[j] = lo;
+    }
+    __syncthreads();
+    for (int p0 = 0; p0 < m; p0 += 8)
+    {
+      const float *bh = reinterpret_cast<const float *>(s_hi + p0 + g);
+      const float *bl = reinterpret_cast<const float *>(s_lo + p0 + g);
+      const uint32_t bhi = __float_as_uint(bh[tq]), blo = __float_as_uint(bl[tq]);
+      float c[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+      for (int blk = 0; blk < 2; ++blk)
+      {
+        mma_k8(c[blk], ahi[2 * blk], ahi[2 * blk + 1], 0u, 0u, blo, 0u);
+        mma_k8(c[blk], ahi[2 * blk], ahi[2 * blk + 1], alo[2 * blk], alo[2 * blk + 1], bhi, bhi);
+      }
+      unsigned mask = 0;
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        mask |= (unsigned)!(c[e >> 2][e & 3] > Trow[2 * (e >> 2) + ((e & 3) >> 1)]) << e;
+      if (__any_sync(kAll, mask != 0))
+      {
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          if ((mask >> e) & 1)
+            atomicOr(&s_mask[warp][(e >> 2) * 16 + ((e & 3) >> 1) * 8 + g],
+                     1u << (2 * tq + (e & 1)));
+        __syncwarp();
+        unsigned bits = s_mask[warp][lane];
+        while (bits)
+        {
+          const int col = __ffs(bits) - 1;
+          bits &= bits - 1;
+          const int pj = p0 + col;
+          if (pj >= m)
+            break;
+          const float4 p = s_pt[pj];
+          if (dist2_pp(qx, qy, qz, p.x, p.y, p.z) <= r2)
+          {
+            if (MODE == kFill || (MODE == kBuffered && count < buffer))
+              dst[count] = __float_as_int(p.w);
+            ++count;
+          }
+        }
+        s_mask[warp][lane] = 0;
+        __syncwarp();
+      }
+    }
+  }
+  if (!active)
+    return;
+  if (MODE != kFill)
+    counts[q] = count;
+  if (MODE == kBuffered && count > buffer)
+    atomicOr(overflow, 1u);
+}
+
 // Nearest with k above 32: a binary heap per query in the output arrays.
 template <int KIND>
 __global__ void __launch_bounds__(kQueryThreads)
@@ -963,7 +1114,21 @@ abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, ForestView const 
 #define ABX_BRUTE(M)                                                                         \
   k_brute_spatial<PRED, M, KIND><<<blocks, kQueryThreads, 0, s>>>(                               \
       t.sorted, t.n, d_preds, nq, d_perm, d_counts, d_offsets, d_out, buffer, d_overflow)
-  if (!t.tnodes) // brute force: every predicate against every value
+#define ABX_BRUTE_TC(M)                                                                    \
+  k_brute_spatial_tc<M><<<blocks, kQueryThreads, 0, s>>>(t.sorted, t.n, d_preds, nq, d_perm,     \
+                                                         d_counts, d_offsets, d_out, buffer,    \
+                                                         d_overflow)
+  if (!t.tnodes && PRED == ABX_SPHERE && KIND == 0 && t.morton_sorted &&
+      tuning_value("BRUTE_TENSOR", 1))
+  {
+    if (mode == kCount)
+      ABX_BRUTE_TC(kCount);
+    else if (mode == kFill)
+      ABX_BRUTE_TC(kFill);
+    else
+      ABX_BRUTE_TC(kBuffered);
+  }
+  else if (!t.tnodes) // brute force: every predicate against every value
   {
     if (mode == kCount)
       ABX_BRUTE(kCount);
@@ -978,6 +1143,7 @@ abx_status spatial_dispatch(cudaStream_t s, TreeView const &t, ForestView const 
     ABX_SPATIAL(kFill);
   else
     ABX_SPATIAL(kBuffered);
+#undef ABX_BRUTE_TC
 #undef ABX_BRUTE
 #undef ABX_SPATIAL
   ABX_CUDA_TRY(cudaGetLastError());

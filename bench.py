@@ -76,7 +76,8 @@ def parse():
     ap.add_argument("--kdop", type=int, default=14, choices=[6, 14, 18, 26],
                     help="--case kdop: KDOP<3, k> of the values")
     ap.add_argument("--case", default="knn",
-                    choices=["knn", "build", "nearest", "radius", "forest", "serve", "kdop", "brute"],
+                    choices=["knn", "build", "nearest", "radius", "forest", "serve", "kdop", "brute",
+                             "brute_radius"],
                     help="knn: the benchmark step (build + kNN); build / nearest / radius: "
                     "one stage alone (profiling cases; radius = 2-pass CRS search with "
                     "~32 expected neighbours)")
@@ -545,7 +546,7 @@ def run_case(args):
     points = torch.from_numpy(points_np).cuda()
     queries = torch.from_numpy(queries_np).cuda()
     r = float(np.float32((32 * 3 / (4 * np.pi * args.n)) ** (1 / 3)))
-    if args.case == "brute":
+    if args.case in ("brute", "brute_radius"):
         bvh = ax.BruteForce(points)
     else:
         bvh = ax.BoundingVolumeHierarchy(points) if args.case != "build" else None

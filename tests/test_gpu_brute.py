@@ -104,13 +104,23 @@ def test_tensor_filter_equals_plain_brute_force(ax, case, k):
         q = (0.5 + 1e-3 * rng.standard_normal((700, 3))).astype(np.float32)
     L = ax._lib.load()
     bf = ax.BruteForce(cuda(p))
+    scale = 1e16 if case == "far" else 1.0
+    radius = np.float32(0.06 * scale if case != "clustered" else 3e-4)
+    spheres = np.concatenate([q, np.full((len(q), 1), radius, np.float32)], axis=1)
+    spheres[::7, 3] = -1.0  # negative radii match nothing
     try:
         ax._lib.check(L.abx_tuning_set(b"BRUTE_TENSOR", 1))
         a = ax.query(bf, ax.nearest(cuda(q), k), with_distances=True)
+        sa = [ax.query(bf, ax.intersects(cuda(spheres)), ax.TraversalPolicy(buf))
+              for buf in (0, 8, -64)] if k == 16 else []
         ax._lib.check(L.abx_tuning_set(b"BRUTE_TENSOR", 0))
         b = ax.query(bf, ax.nearest(cuda(q), k), with_distances=True)
+        sb = [ax.query(bf, ax.intersects(cuda(spheres)), ax.TraversalPolicy(buf))
+              for buf in (0, 8, -64)] if k == 16 else []
     finally:
         L.abx_tuning_reset()
+    for x, y in zip(sa, sb):
+        assert torch.equal(x[0], y[0]) and torch.equal(x[1], y[1])
     for x, y in zip(a, b):
         assert torch.equal(x.view(torch.int32) if x.dtype == torch.float32 else x,
                            y.view(torch.int32) if y.dtype == torch.float32 else y)
