@@ -647,7 +647,8 @@ __global__ void __launch_bounds__(kQueryThreads)
                        const uint32_t *__restrict__ perm,
                        const int32_t *__restrict__ kq, int32_t k_all,
                        const int32_t *__restrict__ offsets, int32_t *__restrict__ offsets_out,
-                       int32_t *__restrict__ out_idx, float *__restrict__ out_dist)
+                       int32_t *__restrict__ out_idx, float *__restrict__ out_dist,
+                       uint64_t *__restrict__ partial)
 {
   constexpr unsigned kAll = 0xffffffffu;
   constexpr int kWarps = kQueryThreads / 32;
@@ -665,8 +666,8 @@ __global__ void __launch_bounds__(kQueryThreads)
   if (active)
   {
     QueryTree tree;
-    task = knn_task(t, n, ForestView{nullptr, nullptr, 1}, tree, nq, perm, kq, k_all,
-                    offsets, offsets_out);
+    task = knn_task(t, n, ForestView{nullptr, nullptr, 1}, tree, nq, perm, kq, k_all, offsets,
+                    blockIdx.y == 0 ? offsets_out : nullptr);
   }
   const bool work = active && task.kk > 0;
   uint64_t key[K];
@@ -705,8 +706,14 @@ __global__ void __launch_bounds__(kQueryThreads)
     s_start = pos;
   }
   __syncthreads();
-  const int64_t num_tiles = (n + kTcTile - 1) / kTcTile;
-  const int64_t start_tile = min(s_start / kTcTile, num_tiles - 1);
+  // this CTA's share of the tiles (gridDim.y chunks when few queries would
+  // leave SMs idle; the partial lists are merged afterwards)
+  const int64_t all_tiles = (n + kTcTile - 1) / kTcTile;
+  const int64_t per_chunk = (all_tiles + gridDim.y - 1) / gridDim.y;
+  const int64_t tile_lo = (int64_t)blockIdx.y * per_chunk;
+  const int64_t num_tiles = max((int64_t)0, min(per_chunk, all_tiles - tile_lo));
+  int64_t start_tile = s_start / kTcTile - tile_lo;
+  start_tile = start_tile < 0 || start_tile >= num_tiles ? 0 : start_tile;
   const float qn = __fadd_rn(__fadd_rn(__fmul_rn(qx, qx), __fmul_rn(qy, qy)), __fmul_rn(qz, qz));
   // a query outside the filter's range takes every pair (T = +inf, NaN pairs
   // count as candidates through !(c > T))
@@ -759,7 +766,7 @@ __global__ void __launch_bounds__(kQueryThreads)
     int64_t tile = start_tile + it;
     if (tile >= num_tiles)
       tile -= num_tiles;
-    const int64_t t0 = tile * kTcTile;
+    const int64_t t0 = (tile_lo + tile) * kTcTile;
     const int m = (int)min((int64_t)kTcTile, n - t0);
     __syncthreads();
     for (int j = threadIdx.x; j < kTcTile; j += blockDim.x)
@@ -840,6 +847,16 @@ __global__ void __launch_bounds__(kQueryThreads)
       }
     }
   }
+  if (partial)
+  {
+    if (active)
+    {
+#pragma unroll
+      for (int m = 0; m < K; ++m)
+        partial[((int64_t)blockIdx.y * nq + t) * K + m] = work ? key[m] : kKeyEmpty;
+    }
+    return;
+  }
   if (!work)
     return;
   const int kk = task.kk;
@@ -848,6 +865,54 @@ __global__ void __launch_bounds__(kQueryThreads)
   {
     const int r = j - first;
     if (r >= 0 && r < kk)
+    {
+      out_idx[task.base + r] = key_value(key[j]);
+      if (out_dist)
+        out_dist[task.base + r] = key_dist(key[j]);
+    }
+  }
+}
+
+// The k best of a query over the point chunks of a split k_brute_nearest_tc
+// launch: the chunks' sorted key lists merged by the same key rule.
+template <int K>
+__global__ void __launch_bounds__(kQueryThreads)
+    k_brute_merge(const uint64_t *__restrict__ partial, int chunks, int64_t n,
+                  int64_t nq, const uint32_t *__restrict__ perm, const int32_t *__restrict__ kq,
+                  int32_t k_all, const int32_t *__restrict__ offsets,
+                  int32_t *__restrict__ out_idx, float *__restrict__ out_dist)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nq)
+    return;
+  QueryTree tree;
+  const KnnTask task = knn_task(t, n, ForestView{nullptr, nullptr, 1}, tree, nq, perm, kq, k_all,
+                                offsets, nullptr);
+  if (task.kk == 0)
+    return;
+  uint64_t key[K];
+  const int first = K - task.k;
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+    key[j] = j < first ? 0ull : kKeyEmpty;
+  for (int c = 0; c < chunks; ++c)
+  {
+    const uint64_t *row = partial + ((int64_t)c * nq + t) * K;
+    for (int m = 0; m < K; ++m)
+    {
+      const uint64_t v = __ldg(row + m);
+      if (v == 0ull || v == kKeyEmpty) // placeholders of k < K, unfilled slots
+        continue;
+      if (!(v < key[K - 1]))
+        break; // the chunk's list is ascending
+      list_insert<K>(key, v);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < K; ++j)
+  {
+    const int r = j - first;
+    if (r >= 0 && r < task.kk)
     {
       out_idx[task.base + r] = key_value(key[j]);
       if (out_dist)
@@ -1161,9 +1226,23 @@ abx_status nearest_k(cudaStream_t s, TreeView const &t, ForestView const &f,
   const int bucket =
       std::max(1, std::min(kMaxBucket, tuning_value("NEAREST_BUCKET", kDefaultNearestBucket)));
   if (!t.tnodes && t.morton_sorted && tuning_value("BRUTE_TENSOR", 1))
-    k_brute_nearest_tc<K><<<blocks, kQueryThreads, 0, s>>>(
+  {
+    // few queries: split the points into chunks so that about two CTAs per
+    // SM run, then merge the chunks' lists
+    const int64_t tiles = (t.n + kTcTile - 1) / kTcTile;
+    const int64_t want = 2 * (int64_t)device_state().num_sms;
+    const int chunks = (int)std::max<int64_t>(
+        1, std::min<int64_t>({tiles, (int64_t)64, (want + blocks - 1) / blocks}));
+    Scratch<uint64_t> partial;
+    if (chunks > 1)
+      ABX_CUDA_TRY(partial.alloc((size_t)chunks * nq * K, s));
+    k_brute_nearest_tc<K><<<dim3(blocks, chunks), kQueryThreads, 0, s>>>(
         t.morton_sorted, t.n, t.morton_codes, t.d_bounds, d_queries, nq, d_perm, d_k, k, d_offsets,
-        d_offsets_out, d_idx, d_dist);
+        d_offsets_out, d_idx, d_dist, chunks > 1 ? partial.ptr : nullptr);
+    if (chunks > 1)
+      k_brute_merge<K><<<blocks, kQueryThreads, 0, s>>>(partial.ptr, chunks, t.n, nq, d_perm, d_k,
+                                                        k, d_offsets, d_idx, d_dist);
+  }
   else if (!t.tnodes) // brute force
     k_brute_nearest<K, KIND><<<blocks, kQueryThreads, 0, s>>>(
         t.sorted, t.n, d_queries, nq, d_k, k, d_offsets, d_offsets_out, d_idx, d_dist);
