@@ -132,3 +132,26 @@ def test_tree_file_with_bad_references_is_refused(tmp_path):
     bad_leaves[1, 3] = np.array([9], np.int32).view(np.float32)[0]
     good_nodes = np.concatenate([node(1, ~2, 2, 1), node(~0, ~1, 1, 1)])
     assert L.abx_bvh_load(None, write(good_nodes, bad_leaves), ctypes.byref(h)) == 1
+
+
+def test_new_entry_points_check_arguments_on_the_host():
+    """Argument checks of the KDOP, gather and host-buffer entry points fail
+    before any device work."""
+    import ctypes
+
+    from arborx_gb300 import _lib
+
+    L = _lib.load()
+    buf = (ctypes.c_float * 64)()
+    # KDOP conversion: source must be points or boxes, target a KDOP kind
+    assert L.abx_kdop_from_geometry(None, _lib.SPHERE, buf, 1, _lib.KDOP14, buf) == 1
+    assert L.abx_kdop_from_geometry(None, _lib.BOX, buf, 1, _lib.BOX, buf) == 1
+    assert L.abx_kdop_from_geometry(None, _lib.POINT, None, 1, _lib.KDOP18, buf) == 1
+    # row gather: whole 32-bit words, non-null arrays
+    assert L.abx_gather_rows(None, buf, 4, 6, buf, 1, buf) == 1
+    assert L.abx_gather_rows(None, buf, 4, 0, buf, 1, buf) == 1
+    assert L.abx_gather_rows(None, None, 4, 16, buf, 1, buf) == 1
+    # KDOP bounds and host-buffer queries need a tree
+    assert L.abx_bvh_kdop_bounds(None, buf) == 1
+    pol = _lib.TraversalPolicyC(0, 1)
+    assert L.abx_bvh_query_nearest_host(None, None, buf, 1, 1, pol, 0, buf, buf, None) == 1
