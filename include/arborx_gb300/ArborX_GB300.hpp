@@ -18,6 +18,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -510,6 +511,26 @@ public:
         _tree.get(), space, reinterpret_cast<const float *>(preds.rays.data()),
         (int64_t)preds.rays.size(), preds.k, c_policy(policy), distances ? 1 : 0, &crs));
     Details::take(space, crs, (int64_t)preds.rays.size(), indices, offsets, distances);
+  }
+
+  // nearest(points, k) with the queries and the CRS in host memory (a
+  // host-side plugin's call; abx_bvh_query_nearest_host): the copies are
+  // pipelined against the traversal.  Returns when the results are on the host.
+  void query_host(cudaStream_t space, std::vector<Point> const &queries, int k,
+                  std::vector<int> &indices, std::vector<int> &offsets,
+                  Experimental::TraversalPolicy const &policy = Experimental::TraversalPolicy(),
+                  std::vector<float> *distances = nullptr) const
+  {
+    const int64_t nq = (int64_t)queries.size();
+    const int64_t kk = std::min<int64_t>(std::max(k, 0), size());
+    offsets.resize((size_t)nq + 1);
+    indices.resize((size_t)(nq * kk));
+    if (distances)
+      distances->resize((size_t)(nq * kk));
+    Details::check(abx_bvh_query_nearest_host(
+        _tree.get(), space, reinterpret_cast<const float *>(queries.data()), nq, k,
+        c_policy(policy), 0, offsets.data(), indices.data(),
+        distances ? distances->data() : nullptr));
   }
 
   abx_bvh const *handle() const { return _tree.get(); }

@@ -377,6 +377,27 @@ static void pair_value_index()
   CHECK((idx == std::vector<int>{107, 108}));
 }
 
+// Host queries and host results: the same CRS as the device query.
+static void host_buffers()
+{
+  std::vector<Point> pts;
+  for (int i = 0; i < 500; ++i)
+    pts.push_back(Point{{(float)(i % 10), (float)((i / 10) % 10), (float)(i / 100)}});
+  BVH tree(nullptr, DeviceView<Point>(pts));
+  std::vector<Point> q = {{{0.2f, 0.1f, 0.3f}}, {{4.4f, 5.6f, 2.1f}}, {{9, 9, 4}}};
+  std::vector<int> hi, ho;
+  std::vector<float> hd;
+  tree.query_host(nullptr, q, 4, hi, ho, Experimental::TraversalPolicy(), &hd);
+  DeviceView<int> di, doff;
+  DeviceView<float> dd;
+  tree.query(nullptr, nearest(DeviceView<Point>(q), 4), di, doff, Experimental::TraversalPolicy(),
+             &dd);
+  CHECK(hi == di.to_host());
+  CHECK(ho == doff.to_host());
+  CHECK(hd == dd.to_host());
+  CHECK((ho == std::vector<int>{0, 4, 8, 12}));
+}
+
 int main()
 {
   empty_tree();
@@ -393,6 +414,7 @@ int main()
   ordered_rays();
   intersects_kdop();
   pair_value_index();
+  host_buffers();
   std::printf("%d checks, %d failures\n", g_checks, g_failures);
   return g_failures == 0 ? 0 : 1;
 }
