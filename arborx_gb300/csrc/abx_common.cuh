@@ -500,6 +500,19 @@ __device__ __forceinline__ int atomic_cas_relaxed(int *addr, int expected, int d
   return old;
 }
 
+// atomicAdd with acquire-release semantics at GPU scope: the adder's earlier
+// stores are visible to whoever later reads the count, and the adder sees
+// the stores that preceded the earlier adds.
+__device__ __forceinline__ unsigned atomic_add_acq_rel(unsigned *addr, unsigned v)
+{
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], %2;"
+               : "=r"(old)
+               : "l"(addr), "r"(v)
+               : "memory");
+  return old;
+}
+
 __device__ __forceinline__ void fence_acq_rel_gpu()
 {
   asm volatile("fence.acq_rel.gpu;" ::: "memory");

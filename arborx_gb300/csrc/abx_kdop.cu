@@ -144,9 +144,10 @@ __global__ void k_kdop_parents(const TNode *__restrict__ tnodes, int64_t nint,
 // Bottom-up KDOP unions.  Thread i writes the records of node i's leaf slots
 // and adds their number to the node's counter; whoever brings a counter to 2
 // owns the node: it forms the union of the two records, writes it into the
-// parent's slot and counts there in turn (release before each count, acquire
-// after it).  The climb ends at the root, which writes the record of the
-// whole tree.
+// parent's slot and counts there in turn (each count an acquire-release
+// atomic add: the counting thread's record stores are released with it, and
+// the owner acquires the other record; records are read through L2).  The
+// climb ends at the root, which writes the record of the whole tree.
 template <int NDIR>
 __global__ void k_kdop_refit(const TNode *__restrict__ tnodes, int64_t nint,
                              const float *__restrict__ kd, int64_t n, const int *__restrict__ parent,
@@ -181,8 +182,7 @@ __global__ void k_kdop_refit(const TNode *__restrict__ tnodes, int64_t nint,
   }
   if (leaves == 0)
     return;
-  fence_acq_rel_gpu();
-  if (atomicAdd(counters + i, leaves) + leaves < 2)
+  if (atomic_add_acq_rel(counters + i, leaves) + leaves < 2)
     return;
   int64_t node = i;
   for (int64_t steps = 0;; ++steps)
@@ -192,7 +192,6 @@ __global__ void k_kdop_refit(const TNode *__restrict__ tnodes, int64_t nint,
       raise_error(err, ABX_DEVERR_INTERNAL);
       return;
     }
-    fence_acq_rel_gpu();
     Kdop<NDIR> a, b;
     kdop_load_cg<NDIR>(knodes + 2 * node * R, a);
     kdop_load_cg<NDIR>(knodes + (2 * node + 1) * R, b);
@@ -209,8 +208,7 @@ __global__ void k_kdop_refit(const TNode *__restrict__ tnodes, int64_t nint,
       return;
     }
     kdop_store<NDIR>(knodes + (int64_t)p * R, a);
-    fence_acq_rel_gpu();
-    if (atomicAdd(counters + (p >> 1), 1u) == 0)
+    if (atomic_add_acq_rel(counters + (p >> 1), 1u) == 0)
       return;
     node = p >> 1;
   }
