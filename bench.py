@@ -75,9 +75,11 @@ def parse():
                     help="--case forest: number of point clouds (trees)")
     ap.add_argument("--kdop", type=int, default=14, choices=[6, 14, 18, 26],
                     help="--case kdop: KDOP<3, k> of the values")
+    ap.add_argument("--grid", type=int, default=64, help="--case rays: cells per axis")
+    ap.add_argument("--rays-per-box", type=int, default=10, help="--case rays: rays per cell")
     ap.add_argument("--case", default="knn",
                     choices=["knn", "build", "nearest", "radius", "forest", "serve", "kdop", "brute",
-                             "brute_radius"],
+                             "brute_radius", "rays", "neighbors"],
                     help="knn: the benchmark step (build + kNN); build / nearest / radius: "
                     "one stage alone (profiling cases; radius = 2-pass CRS search with "
                     "~32 expected neighbours)")
@@ -651,6 +653,174 @@ def run_kdop(args):
     }), flush=True)
 
 
+def timed_steps(fn, warmup, steps):
+    """Mean CUDA-event time (ms) of `steps` calls of fn after `warmup`
+    untimed ones, and the last call's result."""
+    import torch
+
+    for _ in range(warmup):
+        keep = fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        keep = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, keep
+
+
+def make_ray_grid(nx, rays_per_box, seed=23):
+    """The scene of the reference's raytracing example
+    (examples/raytracing/example_raytracing.cpp:218-280): an nx^3 grid of
+    cells of side 100 / nx covering [0, 100]^3 (cell id i + nx j + nx^2 k,
+    corners i * dx computed in float32), and rays_per_box rays per cell from a
+    uniform point of the cell in a uniform direction on the sphere (azimuth
+    U[0, 2 pi), polar angle acos(1 - 2 U[0, 1))).  Seeded numpy draws stand in
+    for the example's Kokkos random pool."""
+    d = np.float32(100.0 / nx)
+    ids = np.arange(nx ** 3, dtype=np.int64)
+    ijk = np.stack([ids % nx, (ids // nx) % nx, ids // (nx * nx)], 1)
+    boxes = np.concatenate([ijk.astype(np.float32) * d, (ijk + 1).astype(np.float32) * d], 1)
+    rng = np.random.default_rng(seed)
+    cell = np.repeat(ids, rays_per_box)
+    org = boxes[cell, :3] + rng.random((cell.size, 3), dtype=np.float32) * d
+    ups = rng.random(cell.size) * 2 * np.pi
+    theta = np.arccos(1 - 2 * rng.random(cell.size))
+    dirs = np.stack([np.cos(ups) * np.sin(theta), np.sin(ups) * np.sin(theta), np.cos(theta)], 1)
+    return boxes, np.concatenate([org, dirs.astype(np.float32)], 1)
+
+
+def run_rays(args):
+    """Ray queries on the raytracing example's scene: build of the cell tree,
+    intersects(Ray) (CRS, hits in depth-first order), ordered_intersects(Ray)
+    (hits by entry distance, with the distances) and nearest(Ray, 1) (first
+    hit).  The CPU leg runs the oracle's brute force on a sample of rays and
+    checks those rays' rows bit for bit."""
+    import torch
+
+    import arborx_gb300 as ax
+    from arborx_gb300 import build as libbuild
+
+    libbuild.build()
+    boxes_np, rays_np = make_ray_grid(args.grid, args.rays_per_box)
+    boxes = torch.from_numpy(boxes_np).cuda()
+    rays = torch.from_numpy(rays_np).cuda()
+    nr = rays.shape[0]
+    ms_build, tree = timed_steps(lambda: ax.BoundingVolumeHierarchy(boxes, kind=ax.BOX),
+                                 args.warmup, args.steps)
+    ms_hit, (ind, off) = timed_steps(lambda: ax.query(tree, ax.ray_intersects(rays)),
+                                     args.warmup, args.steps)
+    ms_ord, (oind, ooff, odist) = timed_steps(
+        lambda: ax.query(tree, ax.ordered_intersects(rays), with_distances=True),
+        args.warmup, args.steps)
+    ms_first, (find, foff) = timed_steps(lambda: ax.query(tree, ax.ordered_intersects(rays, k=1)),
+                                         args.warmup, args.steps)
+    hits = int(off[-1])
+    out = {
+        "case": "rays", "grid": args.grid, "cells": int(boxes.shape[0]), "rays": int(nr),
+        "scene": "raytracing example: cells of side 100/grid, rays from uniform points of each "
+                 "cell in uniform directions",
+        "build_ms": ms_build,
+        "query_ms": {"intersects": ms_hit, "ordered_intersects": ms_ord, "nearest_k1": ms_first},
+        "rays_per_s": {"intersects": nr / (ms_hit * 1e-3), "ordered_intersects": nr / (ms_ord * 1e-3),
+                       "nearest_k1": nr / (ms_first * 1e-3)},
+        "hits_per_ray": hits / nr,
+        "ordered_hits_equal": int(ooff[-1]) == hits,
+        "first_hit_rays": int(foff[-1]),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+
+        sample = np.linspace(0, nr - 1, 256).astype(np.int64)
+        nrm = orc.ray_normalize(rays_np[sample])
+        t0 = time.perf_counter()
+        ro, ri, rd = orc.ray_brute(boxes_np, nrm, ordered=True, is_box=True)
+        t1 = time.perf_counter()
+        uo, ui, _ = orc.ray_brute(boxes_np, nrm, ordered=False, is_box=True)
+        oo, uoff = ooff.cpu().numpy(), off.cpu().numpy()
+        ok = True
+        for j, q in enumerate(sample.tolist()):
+            a, b = int(oo[q]), int(oo[q + 1])
+            ok = ok and np.array_equal(oind[a:b].cpu().numpy(), ri[ro[j]:ro[j + 1]])
+            ok = ok and np.array_equal(odist[a:b].cpu().numpy().view(np.int32),
+                                       rd[ro[j]:ro[j + 1]].view(np.int32))
+            a, b = int(uoff[q]), int(uoff[q + 1])
+            ok = ok and np.array_equal(np.sort(ind[a:b].cpu().numpy()), ui[uo[j]:uo[j + 1]])
+        out["cpu_baseline"] = {
+            "value": len(sample) / (t1 - t0), "unit": "rays/s", "cores": 1, "kind": "port",
+            "sample": "ordered_intersects of %d evenly spaced rays by the oracle's brute force "
+                      "over all cells" % len(sample),
+            "parity": {"rays_checked": len(sample), "bit_exact": bool(ok),
+                       "rule": "ordered rows (index, distance bits); intersects rows as sets"},
+        }
+    print(json.dumps(out), flush=True)
+
+
+def run_neighbors(args):
+    """Radius self-join on n points (r for ~32 neighbours, as the radius
+    case): findFullNeighborList, findHalfNeighborList and expandHalfToFull of
+    the half list.  The CPU leg runs the oracle tree's sphere queries on a
+    sample of the points and checks the first 2000 full rows bit for bit."""
+    import torch
+
+    import arborx_gb300 as ax
+    from arborx_gb300 import build as libbuild
+
+    libbuild.build()
+    points_np, _ = make_inputs(args.n, 1, 0, args.dist)
+    pts = torch.from_numpy(points_np).cuda()
+    n = args.n
+    r = float(np.float32((32 * 3 / (4 * np.pi * n)) ** (1 / 3)))
+    ms_full, (off, ind) = timed_steps(lambda: ax.find_full_neighbor_list(pts, r),
+                                      args.warmup, args.steps)
+    ms_half, (hoff, hind) = timed_steps(lambda: ax.find_half_neighbor_list(pts, r),
+                                        args.warmup, args.steps)
+    ms_exp, (eoff, eind) = timed_steps(lambda: ax.expand_half_to_full(hoff, hind),
+                                       args.warmup, args.steps)
+    pairs = int(off[-1])
+    off_h, eoff_h = off.cpu().numpy(), eoff.cpu().numpy()
+    same = int(eoff_h[-1]) == pairs
+    for i in np.linspace(0, n - 1, 2000).astype(np.int64).tolist():
+        a = np.sort(ind[int(off_h[i]):int(off_h[i + 1])].cpu().numpy())
+        b = np.sort(eind[int(eoff_h[i]):int(eoff_h[i + 1])].cpu().numpy())
+        same = same and np.array_equal(a, b)
+    out = {
+        "case": "neighbors", "dist": args.dist, "n": n, "radius": r,
+        "ms": {"full": ms_full, "half": ms_half, "expand_half_to_full": ms_exp},
+        "points_per_s": {"full": n / (ms_full * 1e-3), "half": n / (ms_half * 1e-3)},
+        "neighbors_per_point": pairs / n, "half_pairs": int(hoff[-1]),
+        "expanded_rows_equal_full_sample": bool(same),
+        "full_list_bytes": 4 * (pairs + n + 1),
+    }
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+
+        m = min(args.cpu_sample, n)
+        sph = np.concatenate([points_np[:m], np.full((m, 1), r, np.float32)], 1)
+        t0 = time.perf_counter()
+        tree = orc.OracleTree(points_np)
+        t1 = time.perf_counter()
+        so, si = tree.spatial(orc.KIND_SPHERE, sph)
+        t2 = time.perf_counter()
+        ok = True
+        for i in range(min(2000, m)):
+            want = si[so[i]:so[i + 1]]
+            got = ind[int(off_h[i]):int(off_h[i + 1])].cpu().numpy()
+            ok = ok and np.array_equal(got, want[want != i])
+        tq = (t2 - t1) * n / m
+        out["cpu_baseline"] = {
+            "value": n / ((t1 - t0) + tq), "unit": "points/s", "cores": orc.num_threads(),
+            "kind": "port",
+            "sample": "oracle tree over all %d points + sphere queries of %d points, query time "
+                      "scaled" % (n, m),
+            "parity": {"rows_checked": min(2000, m), "bit_exact": bool(ok),
+                       "rule": "full row = the tree's sphere row without the point itself"},
+        }
+    print(json.dumps(out), flush=True)
+
+
 def make_clouds(ncl):
     """The batched workload: ncl clouds of floor(10^U(2,5)) points (seed 13);
     cloud i has its lower corner in U[0,100)^3 and extents 10^U(-1,1) per axis
@@ -852,6 +1022,10 @@ def main():
         run_serve(args)
     elif args.case == "kdop":
         run_kdop(args)
+    elif args.case == "rays":
+        run_rays(args)
+    elif args.case == "neighbors":
+        run_neighbors(args)
     elif args.case != "knn":
         run_case(args)
     else:
