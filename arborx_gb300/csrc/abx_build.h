@@ -187,6 +187,17 @@ abx_status order_ray_results(cudaStream_t s, abx_geometry leaf_kind, const float
                              int32_t *d_new_offsets, int32_t *d_out_idx, float *d_out_dist,
                              int64_t *h_new_total);
 
+// nearest(Ray, k) for 1 <= k <= kRayNearestMaxK on a tree of n >= 1 leaves,
+// by a pruned walk (no full hit list): the same rows as the first k of
+// ordered_intersects.  Offsets into d_offsets (nq + 1); indices and, when
+// with_dist, distances allocated on s (*d_idx, *d_dist; released with
+// dfree); the total in *h_total (synchronises s).
+constexpr int kRayNearestMaxK = 32;
+abx_status ray_nearest(cudaStream_t s, abx_geometry leaf_kind, const TNode *d_nodes,
+                       const float4 *d_sorted, int64_t n, const float *d_rays, int64_t nq,
+                       const uint32_t *d_perm, int32_t k, bool with_dist, int32_t *d_offsets,
+                       int32_t **d_idx, float **d_dist, int64_t *h_total);
+
 // The queries whose result count (from CRS offsets) exceeds `buffer`, into
 // d_list (nq entries of room); their number in *h_count (synchronises s).
 abx_status launch_overflow_list(cudaStream_t s, const int32_t *d_offsets, int64_t nq,

@@ -1493,6 +1493,36 @@ abx_status abx_bvh_query_ordered_intersects(const abx_bvh *bvh, void *stream, co
   Scratch<float> rays;
   ABX_CUDA_TRY(rays.alloc((size_t)std::max<int64_t>(nq, 1) * 6, s));
   ABX_TRY(ray_normalize(s, d_rays, nq, rays.ptr));
+  if (k >= 1 && k <= kRayNearestMaxK && bvh->n >= 1 && bvh->tnodes &&
+      tuning_value("RAY_NEAREST", 1))
+  {
+    // nearest(Ray, k): a pruned walk keeps each ray's first k hits, with no
+    // full hit list and no ordering pass (same rows)
+    Scratch<uint32_t> perm;
+    if (policy.sort_predicates && nq > 1)
+      ABX_TRY(sort_predicates(s, bvh, ABX_RAY, rays.ptr, nq, nullptr, perm));
+    abx_crs *c = new (std::nothrow) abx_crs;
+    if (!c)
+      return fail(ABX_ERROR_OUT_OF_MEMORY, "abx_crs");
+    cudaGetDevice(&c->device);
+    c->stream = s;
+    c->nq = nq;
+    int64_t total = 0;
+    abx_status st = dmalloc_n(&c->offsets, nq + 1, s) == cudaSuccess
+                        ? ray_nearest(s, bvh->kind, bvh->tnodes, bvh->sorted, bvh->n, rays.ptr,
+                                      nq, perm.ptr, k, with_distances != 0, c->offsets,
+                                      &c->indices, &c->distances, &total)
+                        : fail(ABX_ERROR_OUT_OF_MEMORY, "CRS");
+    if (st != ABX_SUCCESS)
+    {
+      cudaStreamSynchronize(s);
+      destroy_crs(c);
+      return st;
+    }
+    c->nres = total;
+    *out = c;
+    return ABX_SUCCESS;
+  }
   abx_crs *raw = nullptr;
   ABX_TRY(query_intersects(bvh, s, ABX_RAY, rays.ptr, nq, nullptr, policy, &raw));
   std::unique_ptr<abx_crs, void (*)(abx_crs *)> hits(raw, destroy_crs);

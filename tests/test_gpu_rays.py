@@ -78,3 +78,66 @@ def test_rays_against_brute_force(ax, leaves):
     want = [r[:3] for r in rows(torch.from_numpy(ro), torch.from_numpy(ri))]
     assert rows(off, ind) == want
     assert ax.device_errors() == 0
+
+
+def _ray_nearest_scene(leaves):
+    """20000 leaves with 100 copies of one leaf (equal distances: ties go by
+    index) and 3000 rays, the first 64 starting on a leaf's upper corner with
+    every direction component negative, so that their entry distance into
+    that leaf is -0."""
+    lo = uniform_points(20000, 41)
+    if leaves == "box":
+        geom = np.concatenate([lo, lo + 0.01 + 0.02 * uniform_points(20000, 42)], axis=1)
+    else:
+        geom = lo.copy()
+    geom[100:200] = geom[50]
+    rays = _random_rays(3000, 43)
+    corner = geom[:64, 3:6] if leaves == "box" else geom[:64, :3]
+    rays[:64, :3] = corner
+    rays[:64, 3:6] = -np.abs(rays[:64, 3:6]) - 0.1
+    return geom, rays
+
+
+@pytest.mark.parametrize("leaves", ["box", "point"])
+@pytest.mark.parametrize("k", [1, 2, 5, 16, 32, 40])
+def test_nearest_rays_pruned_walk(ax, leaves, k):
+    """nearest(Ray, k) (a pruned walk for k <= 32) gives the first k entries
+    of each ordered_intersects row: indices and distance bits, -0 included,
+    equal to the oracle's and to the rows of the full ordering pass."""
+    geom, rays = _ray_nearest_scene(leaves)
+    tree = (ax.BoundingVolumeHierarchy(cuda(geom), kind=ax.BOX) if leaves == "box"
+            else ax.BoundingVolumeHierarchy(cuda(geom)))
+    ro, ri, rd = o.ray_brute(geom, o.ray_normalize(rays), ordered=True, is_box=leaves == "box")
+    want_i = [ri[ro[q]:ro[q + 1]][:k].tolist() for q in range(len(rays))]
+    want_d = [rd[ro[q]:ro[q + 1]][:k].view(np.int32).tolist() for q in range(len(rays))]
+    assert any(np.signbit(rd[ro[q]]) for q in range(64) if ro[q + 1] > ro[q])
+    ind, off, dist = ax.query(tree, ax.ordered_intersects(cuda(rays), k=k), with_distances=True)
+    assert rows(off, ind) == want_i
+    assert rows(off, dist.view(torch.int32)) == want_d
+    # the same rows from the ordering pass, and without the distances
+    L = ax._lib.load()
+    try:
+        ax._lib.check(L.abx_tuning_set(b"RAY_NEAREST", 0))
+        ind0, off0, dist0 = ax.query(tree, ax.ordered_intersects(cuda(rays), k=k),
+                                     with_distances=True)
+    finally:
+        L.abx_tuning_reset()
+    assert torch.equal(off0, off) and torch.equal(ind0, ind)
+    assert torch.equal(dist0.view(torch.int32), dist.view(torch.int32))
+    ind1, off1 = ax.query(tree, ax.ordered_intersects(cuda(rays), k=k),
+                          ax.TraversalPolicy(sort_predicates=False))
+    assert torch.equal(off1, off) and torch.equal(ind1, ind)
+    assert ax.device_errors() == 0
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 40])
+def test_nearest_rays_small_trees(ax, n):
+    """One-leaf and small trees; rays that miss everything get empty rows."""
+    geom = np.concatenate([uniform_points(n, 50), uniform_points(n, 50) + 0.2], axis=1)
+    tree = ax.BoundingVolumeHierarchy(cuda(geom), kind=ax.BOX)
+    rays = _random_rays(500, 51)
+    ro, ri, _ = o.ray_brute(geom, o.ray_normalize(rays), ordered=True, is_box=True)
+    for k in (1, 3):
+        ind, off = ax.query(tree, ax.ordered_intersects(cuda(rays), k=k))
+        assert rows(off, ind) == [ri[ro[q]:ro[q + 1]][:k].tolist() for q in range(len(rays))]
+    assert ax.device_errors() == 0
