@@ -354,11 +354,19 @@ __global__ void __launch_bounds__(kQueryThreads)
   }
   int32_t count = 0;
   const int32_t own_pos = FILTER == kEarlierLeaves ? __ldg(leaf_pos + q) : 0;
+  // kEarlierLeaves: the walk reaches leaves in Morton order (left child
+  // first, buckets scanned in order), so after a passing leaf at or past the
+  // query's own position every later leaf is filtered too: the walk ends
+  // there (in the reference, the half traversal starts at the leaf's rope)
+  bool done = false;
   auto emit = [&](int v) {
     if (FILTER == kSkipSelf && v == q)
       return;
     if (FILTER == kEarlierLeaves && __ldg(leaf_pos + v) >= own_pos)
+    {
+      done = true;
       return;
+    }
     if (MODE == kFill)
       dst[count] = v;
     if (MODE == kBuffered && count < cap)
@@ -477,7 +485,7 @@ __global__ void __launch_bounds__(kQueryThreads)
       else
         raise_error(err, ABX_DEVERR_STACK_OVERFLOW);
     }
-    while (!has_next && sp > 0)
+    while (!has_next && sp > 0 && !done)
     {
       --sp;
       if (visit(sref[sp], scf[sp]))
@@ -486,7 +494,7 @@ __global__ void __launch_bounds__(kQueryThreads)
         has_next = true;
       }
     }
-    if (!has_next)
+    if (!has_next || done)
       break;
     node = next;
   }
