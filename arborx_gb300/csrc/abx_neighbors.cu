@@ -1,7 +1,8 @@
 // abx_neighbors.cu -- kernels of the radius self-join neighbor lists
 // (src/spatial/detail/ArborX_NeighborList.hpp:47-188) and of the half-to-full
 // expansion (ArborX_ExpandHalfToFull.hpp:23-69).  The traversal itself is the
-// spatial kernel with a leaf filter (abx_query.cu).
+// spatial kernel with a leaf filter (k_spatial in abx_spatial.cuh, launched
+// from abx_query.cu; the half list's walk ends at the point's own leaf).
 #include "abx_build.h"
 
 namespace abx

@@ -1,7 +1,8 @@
 // abx_spatial.cuh -- the spatial traversal kernel k_spatial and what it
 // shares with the nearest kernels: the query's tree, node loads, the exact
 // squared-distance threshold and the predicate types.  Included by the query
-// translation units (abx_query.cu; abx_kdop.cu instantiates the KDOP forms).
+// translation units (abx_query.cu; abx_kdop.cu instantiates the KDOP forms;
+// abx_rays.cu uses the node loads and the ray predicate for nearest(Ray, k)).
 //
 //   k_spatial   intersects(Sphere | Box | Ray | KDOP) predicates, one thread
 //               per query, depth-first with the left subtree first and the

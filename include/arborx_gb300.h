@@ -454,8 +454,10 @@ ABX_API abx_status abx_server_reset_stats(abx_server *srv);
  * (ArborX_Ray.hpp:435-447, the entry distance), equal distances by value
  * (the reference reports them in heap order).  k > 0 keeps the first k per
  * ray, which is nearest(Ray, k) (leaves the ray misses are never
- * candidates).  d_rays: nq rows of ABX_RAY.  with_distances keeps the
- * distances (abx_crs_distances).  Synchronises the stream. */
+ * candidates).  For 1 <= k <= 32 on a tree the first k come from a pruned
+ * walk that never lists the other hits (same rows and distances).
+ * d_rays: nq rows of ABX_RAY.  with_distances keeps the distances
+ * (abx_crs_distances).  Synchronises the stream. */
 ABX_API abx_status abx_bvh_query_ordered_intersects(const abx_bvh *bvh, void *stream,
                                                     const float *d_rays, int64_t nq, int32_t k,
                                                     abx_traversal_policy policy,
