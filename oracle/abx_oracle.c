@@ -1508,3 +1508,119 @@ int64_t abxo_kdop_spatial_brute(const float *values, int64_t n, int vkind, int v
   }
   return total;
 }
+
+/* TreeTraversal<OrderedSpatial>::operator() (spatial/detail/
+ * ArborX_TreeTraversal.hpp:406-488) restated step for step: distance(Ray,
+ * Box) (ArborX_Ray.hpp:435-447) of both children of an internal node; the
+ * closer one (ties -> the right child) is visited next unless the queue's
+ * top is strictly closer, in which case the top is popped and the closer
+ * child queued; the further child is queued when its distance is finite; a
+ * leaf is reported, then the walk continues from the popped top or ends on
+ * an empty queue.  The queue is ArborX's PriorityQueue with CompareDistance
+ * (lhs.second > rhs.second, the nearest on top), kept here as the max-heap
+ * above over negated distances, which makes the same comparisons and so the
+ * same tie order.  Point leaves are degenerate boxes.  The one-leaf tree
+ * follows :388-401.  Reports (value, distance) in callback order; `heap` has
+ * room for 2n entries (the reference's buffer holds 64). */
+static int64_t ray_ordered_walk(const tree_t *t, const float *ray, pair_t *heap,
+                                int32_t *idx, float *dist, int64_t cap)
+{
+  int64_t count = 0;
+  float b[6];
+#define ABXO_REPORT(v, d)                                                      \
+  do                                                                           \
+  {                                                                            \
+    if (count < cap)                                                           \
+    {                                                                          \
+      idx[count] = (v);                                                        \
+      dist[count] = (d);                                                       \
+    }                                                                          \
+    ++count;                                                                   \
+  } while (0)
+  if (t->n == 0)
+    return 0;
+  if (t->n == 1)
+  {
+    node_box(t, 0, b);
+    const float d = abxo_ray_box_distance(ray, b);
+    if (d != INFINITY)
+      ABXO_REPORT(t->leaves[0].value, d);
+    return count;
+  }
+  int64_t hs = 0;
+  int node = (int)t->n;
+  while (1)
+  {
+    if (node < t->n)
+    {
+      node_box(t, node, b);
+      ABXO_REPORT(t->leaves[node].value, abxo_ray_box_distance(ray, b));
+      if (hs == 0)
+        return count;
+      node = heap[0].idx;
+      heap_pop(heap, hs);
+      --hs;
+    }
+    else
+    {
+      const int left = t->internal[node - t->n].left_child;
+      const int right = node_rope(t, left);
+      node_box(t, left, b);
+      const float dl = abxo_ray_box_distance(ray, b);
+      node_box(t, right, b);
+      const float dr = abxo_ray_box_distance(ray, b);
+      const pair_t lp = {left, dl}, rp = {right, dr};
+      const pair_t closer = dl < dr ? lp : rp;
+      const pair_t further = dl < dr ? rp : lp;
+      if (hs > 0 && -heap[0].dist < closer.dist)
+      {
+        node = heap[0].idx;
+        heap_pop(heap, hs);
+        --hs;
+        if (closer.dist < INFINITY)
+          heap_push(heap, &hs, (pair_t){closer.idx, -closer.dist});
+      }
+      else
+        node = closer.idx;
+      if (further.dist < INFINITY)
+        heap_push(heap, &hs, (pair_t){further.idx, -further.dist});
+    }
+  }
+#undef ABXO_REPORT
+}
+
+/* CRS of the restated ordered traversal for nq normalized rays: indices NULL
+ * fills offsets (nq + 1) and returns the total; then a second call fills
+ * indices and dist (callback order). */
+int64_t abxo_ray_ordered_tree(int64_t n, int is_box, const float *geom, const abxo_leaf *leaves,
+                              const abxo_internal *internal, const float *rays, int64_t nq,
+                              int32_t *offsets, int32_t *indices, float *dist)
+{
+  tree_t t = {n, is_box, geom, leaves, internal};
+  const int64_t hcap = 2 * (n > 0 ? n : 1) + 2;
+#pragma omp parallel
+  {
+    pair_t *heap = (pair_t *)malloc(sizeof(pair_t) * (size_t)hcap);
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t q = 0; q < nq; ++q)
+    {
+      if (!indices)
+        offsets[q] = (int32_t)ray_ordered_walk(&t, rays + 6 * q, heap, NULL, NULL, 0);
+      else
+        ray_ordered_walk(&t, rays + 6 * q, heap, indices + offsets[q], dist + offsets[q],
+                         offsets[q + 1] - offsets[q]);
+    }
+    free(heap);
+  }
+  if (indices)
+    return offsets[nq];
+  int64_t sum = 0;
+  for (int64_t q = 0; q < nq; ++q)
+  {
+    const int64_t c = offsets[q];
+    offsets[q] = (int32_t)sum;
+    sum += c;
+  }
+  offsets[nq] = (int32_t)sum;
+  return sum;
+}

@@ -98,6 +98,8 @@ def lib():
         L.abxo_ray_box_distance.argtypes = [P, P]
         L.abxo_ray_brute.restype = I64
         L.abxo_ray_brute.argtypes = [P, I64, I, P, I64, I, P, P, P]
+        L.abxo_ray_ordered_tree.restype = I64
+        L.abxo_ray_ordered_tree.argtypes = [I64, I, P, P, P, P, I64, P, P, P]
         L.abxo_num_threads.restype = I
         L.abxo_set_num_threads.argtypes = [I]
         _lib = L
@@ -297,6 +299,20 @@ class OracleTree:
         )
         if r < 0:
             raise RuntimeError("oracle nearest traversal overflowed its 64-entry stack")
+        return offsets, indices, dist
+
+    def ray_ordered(self, rays):
+        """CRS (offsets, indices, distances) of ordered_intersects(Ray) by the
+        reference's best-first traversal restated step for step
+        (ArborX_TreeTraversal.hpp:338-489), in its report order; rays
+        already normalized."""
+        r = _f32(rays, 6)
+        nq = r.shape[0]
+        offsets = np.zeros(nq + 1, np.int32)
+        total = lib().abxo_ray_ordered_tree(*self._tree_args(), _p(r), nq, _p(offsets), None, None)
+        indices = np.empty(total, np.int32)
+        dist = np.empty(total, np.float32)
+        lib().abxo_ray_ordered_tree(*self._tree_args(), _p(r), nq, _p(offsets), _p(indices), _p(dist))
         return offsets, indices, dist
 
 
