@@ -765,8 +765,14 @@ static inline float nearest_dist(const tree_t *t, const float q[3], int node)
  * only when strictly closer than the current k-th distance, the closer child
  * is visited first (ties -> left), and the final order is the heap sort's.
  * `buf` has room for k pairs.  Returns the number of results (min(k, n)). */
+static int64_t nearest_arborx_walk(const tree_t *t, const float *q, int is_ray, int k,
+                                   pair_t *buf, int64_t *visits);
+
 static int64_t nearest_arborx_counted(const tree_t *t, const float q[3], int k,
-                                      pair_t *buf, int64_t *visits);
+                                      pair_t *buf, int64_t *visits)
+{
+  return nearest_arborx_walk(t, q, 0, k, buf, visits);
+}
 
 static int64_t nearest_arborx(const tree_t *t, const float q[3], int k,
                               pair_t *buf)
@@ -774,18 +780,32 @@ static int64_t nearest_arborx(const tree_t *t, const float q[3], int k,
   return nearest_arborx_counted(t, q, k, buf, NULL);
 }
 
+float abxo_ray_box_distance(const float *ray, const float *box);
+
+/* distance(predicate geometry, node): a point (q[0..2]) or a normalized ray
+ * (q[0..5], distance(Ray, Box) of ArborX_Ray.hpp:435-447, point leaves as
+ * degenerate boxes). */
+static inline float walk_dist(const tree_t *t, const float *q, int is_ray, int node)
+{
+  if (!is_ray)
+    return nearest_dist(t, q, node);
+  float b[6];
+  node_box(t, node, b);
+  return abxo_ray_box_distance(q, b);
+}
+
 /* visits (optional): [0] internal nodes read (root + internal children whose
  * distance is computed), [1] leaves read (leaf children whose distance is
  * computed).  These are the node reads of the reference traversal. */
-static int64_t nearest_arborx_counted(const tree_t *t, const float q[3], int k,
-                                      pair_t *buf, int64_t *visits)
+static int64_t nearest_arborx_walk(const tree_t *t, const float *q, int is_ray, int k,
+                                   pair_t *buf, int64_t *visits)
 {
   if (k < 1 || t->n == 0)
     return 0;
   if (t->n == 1)
   {
     buf[0].idx = 0;
-    buf[0].dist = nearest_dist(t, q, 0);
+    buf[0].dist = walk_dist(t, q, is_ray, 0);
     return 1;
   }
   int64_t hsize = 0;
@@ -813,8 +833,8 @@ static int64_t nearest_arborx_counted(const tree_t *t, const float q[3], int k,
         visits[left_child < t->n ? 1 : 0]++;
         visits[right_child < t->n ? 1 : 0]++;
       }
-      distance_left = nearest_dist(t, q, left_child);
-      distance_right = nearest_dist(t, q, right_child);
+      distance_left = walk_dist(t, q, is_ray, left_child);
+      distance_right = walk_dist(t, q, is_ray, right_child);
       if (distance_left < radius)
       {
         if (left_child < t->n)
@@ -1612,6 +1632,60 @@ int64_t abxo_ray_ordered_tree(int64_t n, int is_box, const float *geom, const ab
     }
     free(heap);
   }
+  if (indices)
+    return offsets[nq];
+  int64_t sum = 0;
+  for (int64_t q = 0; q < nq; ++q)
+  {
+    const int64_t c = offsets[q];
+    offsets[q] = (int32_t)sum;
+    sum += c;
+  }
+  offsets[nq] = (int32_t)sum;
+  return sum;
+}
+
+/* nearest(Ray, k) by the reference's nearest traversal
+ * (ArborX_TreeTraversal.hpp:122-336, the verbatim walk above with
+ * distance(Ray, Box)): candidates only at a distance below the current k-th
+ * (so a missed leaf, at +inf, never enters on a tree of two or more leaves;
+ * the one-leaf tree reports its leaf whatever the distance, :158-167), in
+ * heap-sort order.  indices NULL fills offsets (nq + 1) and returns the
+ * total; a second call fills indices and dist.  Returns -1 if a walk would
+ * overflow the reference's 64-entry stack. */
+int64_t abxo_ray_nearest_arborx(int64_t n, int is_box, const float *geom,
+                                const abxo_leaf *leaves, const abxo_internal *internal,
+                                const float *rays, int64_t nq, int k, int32_t *offsets,
+                                int32_t *indices, float *dist)
+{
+  tree_t t = {n, is_box, geom, leaves, internal};
+  int failed = 0;
+#pragma omp parallel
+  {
+    pair_t *buf = (pair_t *)malloc(sizeof(pair_t) * (size_t)(k > 0 ? k : 1));
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t q = 0; q < nq; ++q)
+    {
+      const int64_t c = nearest_arborx_walk(&t, rays + 6 * q, 1, k, buf, NULL);
+      if (c < 0)
+      {
+#pragma omp atomic write
+        failed = 1;
+        continue;
+      }
+      if (!indices)
+        offsets[q] = (int32_t)c;
+      else
+        for (int64_t j = 0; j < c; ++j)
+        {
+          indices[offsets[q] + j] = buf[j].idx;
+          dist[offsets[q] + j] = buf[j].dist;
+        }
+    }
+    free(buf);
+  }
+  if (failed)
+    return -1;
   if (indices)
     return offsets[nq];
   int64_t sum = 0;

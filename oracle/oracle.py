@@ -100,6 +100,8 @@ def lib():
         L.abxo_ray_brute.argtypes = [P, I64, I, P, I64, I, P, P, P]
         L.abxo_ray_ordered_tree.restype = I64
         L.abxo_ray_ordered_tree.argtypes = [I64, I, P, P, P, P, I64, P, P, P]
+        L.abxo_ray_nearest_arborx.restype = I64
+        L.abxo_ray_nearest_arborx.argtypes = [I64, I, P, P, P, P, I64, I, P, P, P]
         L.abxo_num_threads.restype = I
         L.abxo_set_num_threads.argtypes = [I]
         _lib = L
@@ -313,6 +315,23 @@ class OracleTree:
         indices = np.empty(total, np.int32)
         dist = np.empty(total, np.float32)
         lib().abxo_ray_ordered_tree(*self._tree_args(), _p(r), nq, _p(offsets), _p(indices), _p(dist))
+        return offsets, indices, dist
+
+    def ray_nearest_arborx(self, rays, k):
+        """CRS (offsets, indices, distances) of nearest(Ray, k) by the
+        reference's nearest traversal restated (ArborX_TreeTraversal.hpp:
+        122-336) with distance(Ray, Box); rays already normalized."""
+        r = _f32(rays, 6)
+        nq = r.shape[0]
+        offsets = np.zeros(nq + 1, np.int32)
+        total = lib().abxo_ray_nearest_arborx(*self._tree_args(), _p(r), nq, int(k), _p(offsets),
+                                              None, None)
+        if total < 0:
+            raise RuntimeError("oracle nearest traversal overflowed its 64-entry stack")
+        indices = np.empty(total, np.int32)
+        dist = np.empty(total, np.float32)
+        lib().abxo_ray_nearest_arborx(*self._tree_args(), _p(r), nq, int(k), _p(offsets),
+                                      _p(indices), _p(dist))
         return offsets, indices, dist
 
 

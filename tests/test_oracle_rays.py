@@ -63,3 +63,29 @@ def test_restated_ordered_traversal_equals_rows_up_to_ties_and_dead_ends():
             assert np.array_equal(i[order], bi[bo[q]:bo[q + 1]])
             assert np.array_equal(d[order].view(np.int32), bd[bo[q]:bo[q + 1]].view(np.int32))
         assert dead_ends > 0
+
+
+def test_restated_nearest_ray_traversal_equals_rows_up_to_ties():
+    """nearest(Ray, k) by the reference's nearest traversal with
+    distance(Ray, Box): the same distances, bit for bit, as the first k of
+    the ordered rows; the indices differ only where the k-th distance is
+    tied with the next hit (the reference keeps the first one it meets, the
+    rows here the smaller value)."""
+    for leaves in ("box", "point"):
+        geom, rays = _scene(leaves)
+        tree = o.OracleTree(geom, is_box=leaves == "box")
+        bo, bi, bd = o.ray_brute(geom, rays, ordered=True, is_box=leaves == "box")
+        for k in (1, 3, 8):
+            no, ni, nd = tree.ray_nearest_arborx(rays, k)
+            for q in range(len(rays)):
+                row_i, row_d = bi[bo[q]:bo[q + 1]], bd[bo[q]:bo[q + 1]]
+                got_i, got_d = ni[no[q]:no[q + 1]], nd[no[q]:no[q + 1]]
+                assert np.array_equal(got_d + np.float32(0), row_d[:k] + np.float32(0))
+                if sorted(got_i.tolist()) != sorted(row_i[:k].tolist()):
+                    assert len(row_d) > k and row_d[k - 1] == row_d[k]
+    # the one-leaf tree reports its leaf whatever the distance (:158-167);
+    # the rows here hold hits only
+    one = o.OracleTree(np.asarray([[0, 0, 0, 1, 1, 1]], np.float32), is_box=True)
+    miss = o.ray_normalize(np.asarray([[4, 5, 6, 7, 8, 9]], np.float32))
+    off, ind, dist = one.ray_nearest_arborx(miss, 1)
+    assert off.tolist() == [0, 1] and ind.tolist() == [0] and dist[0] == np.inf
