@@ -692,12 +692,50 @@ def make_ray_grid(nx, rays_per_box, seed=23):
     return boxes, np.concatenate([org, dirs.astype(np.float32)], 1)
 
 
+def ray_cpu_leg(boxes_np, rays_np, timed_rays, ordered_row, hit_row, checked=256):
+    """CPU leg of the ray case: the reference's ordered traversal restated in
+    the oracle (tree over all cells, then ordered_intersects of `timed_rays`
+    evenly spaced rays on all host threads, ray time scaled to every ray),
+    and a bit-for-bit check of `checked` evenly spaced rays: ordered_row(q)
+    (indices, distances) against the oracle's brute-force ordering, hit_row(q)
+    (intersects) against its hits as a set."""
+    from oracle import oracle as orc
+
+    nr = len(rays_np)
+    timed = np.linspace(0, nr - 1, max(1, timed_rays)).astype(np.int64)
+    nrm = orc.ray_normalize(rays_np[timed])
+    t0 = time.perf_counter()
+    tree = orc.OracleTree(boxes_np, is_box=True)
+    t1 = time.perf_counter()
+    tree.ray_ordered(nrm)
+    t2 = time.perf_counter()
+    sample = np.linspace(0, nr - 1, min(checked, nr)).astype(np.int64)
+    snrm = orc.ray_normalize(rays_np[sample])
+    ro, ri, rd = orc.ray_brute(boxes_np, snrm, ordered=True, is_box=True)
+    uo, ui, _ = orc.ray_brute(boxes_np, snrm, ordered=False, is_box=True)
+    ok = True
+    for j, q in enumerate(sample.tolist()):
+        gi, gd = ordered_row(q)
+        ok = ok and np.array_equal(gi, ri[ro[j]:ro[j + 1]])
+        ok = ok and np.array_equal(np.asarray(gd, np.float32).view(np.int32),
+                                   rd[ro[j]:ro[j + 1]].view(np.int32))
+        ok = ok and np.array_equal(np.sort(hit_row(q)), ui[uo[j]:uo[j + 1]])
+    return {
+        "value": nr / ((t1 - t0) + (t2 - t1) * nr / len(timed)), "unit": "rays/s",
+        "cores": orc.num_threads(), "kind": "port",
+        "sample": "the reference's ordered traversal restated: tree over all %d cells + "
+                  "ordered_intersects of %d of %d rays, ray time scaled" % (len(boxes_np), len(timed), nr),
+        "parity": {"rays_checked": len(sample), "bit_exact": bool(ok),
+                   "rule": "ordered rows (index, distance bits) vs brute force; intersects rows as sets"},
+    }
+
+
 def run_rays(args):
     """Ray queries on the raytracing example's scene: build of the cell tree,
     intersects(Ray) (CRS, hits in depth-first order), ordered_intersects(Ray)
     (hits by entry distance, with the distances) and nearest(Ray, 1) (first
-    hit).  The CPU leg runs the oracle's brute force on a sample of rays and
-    checks those rays' rows bit for bit."""
+    hit).  The CPU leg (ray_cpu_leg) times the reference's ordered traversal
+    restated in the oracle and checks a sample of rays' rows bit for bit."""
     import torch
 
     import arborx_gb300 as ax
@@ -731,30 +769,17 @@ def run_rays(args):
         "first_hit_rays": int(foff[-1]),
     }
     if not args.no_cpu_baseline:
-        from oracle import oracle as orc
+        oo, uo = ooff.cpu().numpy(), off.cpu().numpy()
 
-        sample = np.linspace(0, nr - 1, 256).astype(np.int64)
-        nrm = orc.ray_normalize(rays_np[sample])
-        t0 = time.perf_counter()
-        ro, ri, rd = orc.ray_brute(boxes_np, nrm, ordered=True, is_box=True)
-        t1 = time.perf_counter()
-        uo, ui, _ = orc.ray_brute(boxes_np, nrm, ordered=False, is_box=True)
-        oo, uoff = ooff.cpu().numpy(), off.cpu().numpy()
-        ok = True
-        for j, q in enumerate(sample.tolist()):
+        def ordered_row(q):
             a, b = int(oo[q]), int(oo[q + 1])
-            ok = ok and np.array_equal(oind[a:b].cpu().numpy(), ri[ro[j]:ro[j + 1]])
-            ok = ok and np.array_equal(odist[a:b].cpu().numpy().view(np.int32),
-                                       rd[ro[j]:ro[j + 1]].view(np.int32))
-            a, b = int(uoff[q]), int(uoff[q + 1])
-            ok = ok and np.array_equal(np.sort(ind[a:b].cpu().numpy()), ui[uo[j]:uo[j + 1]])
-        out["cpu_baseline"] = {
-            "value": len(sample) / (t1 - t0), "unit": "rays/s", "cores": 1, "kind": "port",
-            "sample": "ordered_intersects of %d evenly spaced rays by the oracle's brute force "
-                      "over all cells" % len(sample),
-            "parity": {"rays_checked": len(sample), "bit_exact": bool(ok),
-                       "rule": "ordered rows (index, distance bits); intersects rows as sets"},
-        }
+            return oind[a:b].cpu().numpy(), odist[a:b].cpu().numpy()
+
+        def hit_row(q):
+            return ind[int(uo[q]):int(uo[q + 1])].cpu().numpy()
+
+        out["cpu_baseline"] = ray_cpu_leg(boxes_np, rays_np, min(args.cpu_sample, nr),
+                                          ordered_row, hit_row)
     print(json.dumps(out), flush=True)
 
 
