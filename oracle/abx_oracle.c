@@ -1698,3 +1698,68 @@ int64_t abxo_ray_nearest_arborx(int64_t n, int is_box, const float *geom,
   offsets[nq] = (int32_t)sum;
   return sum;
 }
+
+/* findHalfNeighborList (spatial/detail/ArborX_NeighborList.hpp:47-111) with
+ * HalfTraversal (ArborX_HalfTraversal.hpp:23-75) restated: the sphere of
+ * leaf i (its point, radius r) walks the ropes from the leaf's own rope, so
+ * only the leaves after it in Morton order, and each leaf it intersects
+ * lists i's value in its row.  Trees of fewer than two leaves list nothing.
+ * Leaves run here by increasing position (the reference runs them in
+ * parallel with atomic row cursors, so its order inside a row is free).
+ * indices NULL fills offsets (n + 1) and returns the total; a second call
+ * fills indices. */
+int64_t abxo_half_neighbors(int64_t n, const float *geom, const abxo_leaf *leaves,
+                            const abxo_internal *internal, float r, int32_t *offsets,
+                            int32_t *indices)
+{
+  tree_t t = {n, 0, geom, leaves, internal};
+  int32_t *cursor = NULL;
+  if (!indices)
+    for (int64_t q = 0; q <= n; ++q)
+      offsets[q] = 0;
+  else
+  {
+    cursor = (int32_t *)malloc(sizeof(int32_t) * (size_t)(n > 0 ? n : 1));
+    for (int64_t q = 0; q < n; ++q)
+      cursor[q] = offsets[q];
+  }
+  for (int64_t i = 0; n >= 2 && i < n; ++i)
+  {
+    const int32_t v1 = leaves[i].value;
+    const float pred[4] = {geom[3 * (int64_t)v1], geom[3 * (int64_t)v1 + 1],
+                           geom[3 * (int64_t)v1 + 2], r};
+    int node = leaves[i].rope;
+    while (node != ABXO_ROPE_SENTINEL)
+    {
+      if (node < n)
+      {
+        if (spatial_test(&t, 1, pred, node))
+        {
+          const int32_t v2 = leaves[node].value;
+          if (!indices)
+            offsets[v2]++;
+          else
+            indices[cursor[v2]++] = v1;
+        }
+        node = leaves[node].rope;
+      }
+      else
+        node = spatial_test(&t, 1, pred, node) ? internal[node - n].left_child
+                                               : internal[node - n].rope;
+    }
+  }
+  if (indices)
+  {
+    free(cursor);
+    return offsets[n];
+  }
+  int64_t sum = 0;
+  for (int64_t q = 0; q < n; ++q)
+  {
+    const int64_t c = offsets[q];
+    offsets[q] = (int32_t)sum;
+    sum += c;
+  }
+  offsets[n] = (int32_t)sum;
+  return sum;
+}

@@ -102,6 +102,8 @@ def lib():
         L.abxo_ray_ordered_tree.argtypes = [I64, I, P, P, P, P, I64, P, P, P]
         L.abxo_ray_nearest_arborx.restype = I64
         L.abxo_ray_nearest_arborx.argtypes = [I64, I, P, P, P, P, I64, I, P, P, P]
+        L.abxo_half_neighbors.restype = I64
+        L.abxo_half_neighbors.argtypes = [I64, P, P, P, ctypes.c_float, P, P]
         L.abxo_num_threads.restype = I
         L.abxo_set_num_threads.argtypes = [I]
         _lib = L
@@ -316,6 +318,20 @@ class OracleTree:
         dist = np.empty(total, np.float32)
         lib().abxo_ray_ordered_tree(*self._tree_args(), _p(r), nq, _p(offsets), _p(indices), _p(dist))
         return offsets, indices, dist
+
+    def half_neighbors(self, radius):
+        """CRS (offsets, indices) of findHalfNeighborList over this point
+        tree by the reference's HalfTraversal restated (ArborX_HalfTraversal.hpp:
+        23-75): row p lists the points within radius whose leaf precedes p's,
+        in Morton order."""
+        assert not self.is_box
+        offsets = np.zeros(self.n + 1, np.int32)
+        total = lib().abxo_half_neighbors(self.n, _p(self.geom), _p(self.leaves), _p(self.internal),
+                                          float(radius), _p(offsets), None)
+        indices = np.empty(total, np.int32)
+        lib().abxo_half_neighbors(self.n, _p(self.geom), _p(self.leaves), _p(self.internal),
+                                  float(radius), _p(offsets), _p(indices))
+        return offsets, indices
 
     def ray_nearest_arborx(self, rays, k):
         """CRS (offsets, indices, distances) of nearest(Ray, k) by the
