@@ -413,6 +413,8 @@ abx_status ray_nearest(cudaStream_t s, abx_geometry leaf_kind, const TNode *d_no
   {
     ABX_CUDA_TRY(cudaMemsetAsync(d_offsets, 0, sizeof(int32_t), s));
     ABX_CUDA_TRY(dmalloc_n(d_idx, 0, s));
+    if (with_dist)
+      ABX_CUDA_TRY(dmalloc_n(d_dist, 0, s));
     return ABX_SUCCESS;
   }
   Scratch<int32_t> counts, dense_idx;
